@@ -4,7 +4,11 @@ TEST INFRASTRUCTURE ONLY.  Compiles the reference's ``KernelDefinitions.h`` +
 ``Kernel.cl`` exactly where they lie in the reference checkout (the same
 concatenation KernelInvoker.cpp:41-45 JIT-compiles), as plain C11 through
 ``ref_shim.h``, and links it with the fiber work-group emulator
-``ref_emu.c``.  Only output: ``oracle/_ref/libref_emu.so`` (git-ignored).
+``ref_emu.c``.  The reference's host ``Tools.cpp`` and ``Logger.cpp`` are
+compiled too (against the OpenCL declarations in ``ref_cl/CL/cl.h``, whose
+entry points are never called) so that ``ref_sort_glue.cpp`` can run the
+reference's own ``preorder_by_x``.  Only output: ``oracle/_ref/libref_emu.so``
+(git-ignored).
 
 One mechanical edit is applied in the pipe to gcc (nothing is written to
 disk): the two work-group-shared arrays declared in the kernel body
@@ -64,8 +68,10 @@ def build(reference: str | None = None, force: bool = False, quiet: bool = False
         if not quiet:
             print(f"reference sources not found under {ref}; oracle/_ref not built", file=sys.stderr)
         return None
-    srcs = [os.path.join(ref, "Kernel.cl"), os.path.join(ref, "KernelDefinitions.h"),
-            os.path.join(HERE, "ref_emu.c"), os.path.join(HERE, "ref_shim.h"), __file__]
+    srcs = [os.path.join(ref, f) for f in ("Kernel.cl", "KernelDefinitions.h", "Tools.cpp", "Logger.cpp")]
+    srcs += [os.path.join(HERE, f) for f in ("ref_emu.c", "ref_shim.h", "ref_sort_glue.cpp",
+                                               "ref_cl/CL/cl.h", "ref_cl/ref_cl_stubs.c")]
+    srcs.append(__file__)
     if (not force and os.path.exists(OUT_LIB)
             and os.path.getmtime(OUT_LIB) >= max(os.path.getmtime(s) for s in srcs)):
         return OUT_LIB
@@ -75,7 +81,16 @@ def build(reference: str | None = None, force: bool = False, quiet: bool = False
     subprocess.run(["gcc", *CFLAGS, "-I", HERE, "-x", "c", "-c", "-", "-o", kobj],
                    input=kernel_source(ref).encode(), check=True)
     subprocess.run(["gcc", *CFLAGS, "-c", os.path.join(HERE, "ref_emu.c"), "-o", eobj], check=True)
-    subprocess.run(["gcc", "-shared", "-o", OUT_LIB, kobj, eobj, "-lpthread", "-lm"], check=True)
+    objs = [kobj, eobj]
+    cl_inc = ["-I", os.path.join(HERE, "ref_cl"), "-I", ref]
+    for src, comp in ((os.path.join(ref, "Tools.cpp"), "g++"), (os.path.join(ref, "Logger.cpp"), "g++"),
+                      (os.path.join(HERE, "ref_sort_glue.cpp"), "g++"),
+                      (os.path.join(HERE, "ref_cl", "ref_cl_stubs.c"), "gcc")):
+        obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
+        std = ["-std=gnu++14"] if comp == "g++" else ["-std=gnu11"]
+        subprocess.run([comp, "-O2", "-fPIC", "-w", *std, *cl_inc, "-c", src, "-o", obj], check=True)
+        objs.append(obj)
+    subprocess.run(["g++", "-shared", "-o", OUT_LIB, *objs, "-lpthread", "-lm"], check=True)
     return OUT_LIB
 
 

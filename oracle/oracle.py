@@ -89,8 +89,19 @@ def ref_lib():
         l.ref_search_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        l.ref_preorder_by_x.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _ref = l
     return _ref
+
+
+def ref_sort_by_x(blobs: Sequence[bytes]) -> List[bytes]:
+    """The reference's own preorder_by_x (Tools.cpp:46-66) over a batch of events."""
+    bufs = [ctypes.create_string_buffer(bytes(b), len(b)) for b in blobs]
+    ptrs = (ctypes.c_void_p * len(bufs))(*[ctypes.addressof(b) for b in bufs])
+    sizes = np.array([len(b) for b in blobs], np.uint64)
+    if ref_lib().ref_preorder_by_x(ptrs, _ptr(sizes), len(blobs)) != 0:
+        raise RuntimeError("reference preorder_by_x failed")
+    return [b.raw for b in bufs]
 
 
 def _ptr(a: np.ndarray):
