@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 search-by-triplet (events/s) on seeded synthetic VELO events.
+
+Default workload: 10,000 events from seeds 1000..10999 of the synthetic VELO
+generator (the plain path at scale: one CTA per event, Y = 4, no FMA
+contraction), x-sorted by the reference sort before timing.
+
+Per step the GPU arm searches the whole batch once:
+  value  device-resident: one kernel launch over events already in HBM, timed
+         with CUDA events on the library's stream; L2 is flushed between steps
+         (a 2 x L2 memset) and the input is also larger than L2.
+  e2e    the public C ABI (velo_search_packed) from pinned host memory:
+         H2D of the events, the kernel, D2H of counts / offsets / status /
+         tracks, all inside the timed region (host wall clock).
+  cpu_baseline  the oracle restatement of the reference algorithm on all host
+         cores over a bounded sample (rank 0 only).
+`--impl reference` times the reference's algorithm on the host CPU instead:
+the reference kernel under the work-group emulator where it was built
+(oracle/_ref), else the oracle restatement.
+
+Multi-GPU (torchrun): weak scaling, every rank searches its own 10,000-event
+block (seeds offset by rank); no collective touches the data path, only a
+barrier and a max-reduction of the step time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "events/s on 1 GB300: plain vs learned-pruned at <=0.5% eff loss; vs ref on host CPU"
+
+CONFIGS = {
+    # name: (first seed, events, generator params attr, launch mode, description)
+    "scale": (1000, 10000, "CONFIG_SCALE", 0,
+              "10,000 synthetic VELO events (seeds 1000-10999), plain path, one CTA per event"),
+    "small": (0, 100, "CONFIG_SMALL", 0, "100 synthetic VELO events (seeds 0-99), one CTA per event"),
+    "batched": (2000000, 100000, "CONFIG_BATCHED", 1,
+                "100,000 uneven events, PVs ~ Poisson(U(2,30)), persistent CTAs"),
+    "stress": (3000000, 100000, "CONFIG_STRESS", 1,
+               "100,000 events at PVs ~ Poisson(30), 2% noise, 0.96 hit efficiency, persistent CTAs"),
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="scale")
+    ap.add_argument("--events", type=int, default=0, help="override the number of events")
+    ap.add_argument("--launch", choices=["per-event", "persistent"], default=None)
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--smem-hits", type=int, default=0)
+    ap.add_argument("--no-narrow", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-emulator", action="store_true",
+                    help="reference arm: time the reference kernel under the work-group emulator "
+                         "(oracle/_ref, only where it was built) instead of the oracle restatement")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- ranks --
+class Ranks:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def shard_seeds(first_seed: int, n_events: int, rank: int) -> range:
+    """Weak scaling: rank r owns its own block of n_events seeds."""
+    start = first_seed + rank * n_events
+    return range(start, start + n_events)
+
+
+# -------------------------------------------------------------- workload --
+def make_workload(args, rank: int):
+    from cl_forward_gb300 import events, generator
+    first, n, params_name, _, _ = CONFIGS[args.config]
+    n = args.events or n
+    raw, truths = generator.generate_parallel(shard_seeds(first, n, rank), getattr(generator, params_name))
+    return raw, truths
+
+
+def sort_events(raw):
+    from oracle import oracle   # sort only: the reference's preorder_by_x, restated
+    return [oracle.sort_by_x(b) for b in raw]
+
+
+def workload_stats(blobs):
+    import numpy as np
+    S = np.array([int(np.frombuffer(b[0:4], "<i4")[0]) for b in blobs])
+    H = np.array([int(np.frombuffer(b[4:8], "<i4")[0]) for b in blobs])
+    return S, H
+
+
+# ---------------------------------------------------------------- clocks --
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[4], parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        maxp = max(r[2] for r in rows)
+        loaded = [r for r in rows if r[2] >= 0.5 * maxp] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in loaded for i, v in enumerate(r[4]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "samples_under_load": len(loaded)}
+
+
+# ------------------------------------------------------------- baselines --
+def cpu_baseline(blobs, seconds: float):
+    """Oracle restatement over all host cores, repeated passes until `seconds`."""
+    from oracle import oracle
+    n = len(blobs)
+    passes, elapsed = 0, 0.0
+    while elapsed < seconds or passes == 0:
+        elapsed += oracle.time_search(blobs, 4, 0)
+        passes += 1
+    cores = os.cpu_count() or 1
+    return {"value": n * passes / elapsed, "unit": "events/s", "cores": cores, "kind": "port",
+            "sample": f"{passes} pass(es) over the same {n} x-sorted events, Y=4, {cores} threads, "
+                      f"{elapsed:.1f} s, search only (sort excluded, as on the GPU)"}
+
+
+def reference_arm(args, ranks: Ranks):
+    if ranks.rank != 0:
+        return None
+    raw, _ = make_workload(args, 0)
+    blobs = sort_events(raw)
+    from oracle import oracle
+    n = len(blobs)
+    kind = "port"
+    run = lambda: oracle.time_search(blobs, 4, 0)
+    try:
+        if args.ref_emulator and os.path.exists(oracle.REF_LIB):
+            oracle.ref_lib()
+            kind = "reference"
+
+            def run():
+                t0 = time.perf_counter()
+                oracle.ref_search(blobs, 4, 0)
+                return time.perf_counter() - t0
+    except Exception:
+        kind = "port"
+    for _ in range(args.warmup):
+        run()
+    total = sum(run() for _ in range(args.steps))
+    value = n * args.steps / total
+    cores = os.cpu_count() or 1
+    what = ("the reference kernel (Kernel.cl) under the work-group emulator" if kind == "reference"
+            else "the oracle restatement of the reference algorithm")
+    _, _, _, _, desc = CONFIGS[args.config]
+    return {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic seeded VELO events (no public dataset)",
+        "config": {"workload": desc, "events": n, "y_lanes": 4},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": cores, "kind": kind,
+                         "sample": f"each step one pass of {what} over all {n} events on {cores} host "
+                                   f"threads ({os.uname().machine})"},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ---------------------------------------------------------------- GPU arm --
+def gpu_arm(args, ranks: Ranks):
+    import numpy as np
+    from cl_forward_gb300 import events as E
+
+    raw, truths = make_workload(args, ranks.rank)          # process pool before any GPU call
+    blobs = sort_events(raw)
+    S, H = workload_stats(blobs)
+    n = len(blobs)
+
+    from cl_forward_gb300 import build, native
+    build.build()
+    ctx = native.Context(ranks.local)
+    mode = CONFIGS[args.config][3] if args.launch is None else (1 if args.launch == "persistent" else 0)
+    opts = native.default_options(threads_per_event=args.threads, launch_mode=mode,
+                                  smem_hits=args.smem_hits, narrow_windows=0 if args.no_narrow else 1)
+
+    # pinned host input, 16-byte aligned events
+    offs = np.zeros(n, np.uint64)
+    sizes = np.array([len(b) for b in blobs], np.uint64)
+    total = 0
+    for i, b in enumerate(blobs):
+        offs[i] = total
+        total += (len(b) + 15) // 16 * 16
+    hbuf = ctx.host_alloc(max(total, 16))
+    for i, b in enumerate(blobs):
+        hbuf[int(offs[i]):int(offs[i]) + len(b)] = np.frombuffer(b, np.uint8)
+
+    # ---- device-resident value ------------------------------------------
+    ctx.stage(hbuf, offs, sizes)
+    ctx.synchronize()
+    ranks.barrier()
+    with Clocks(ranks.local) as clk:
+        ms = ctx.time_runs(opts, warmup=args.warmup, iters=args.steps, flush_l2=True)
+    ranks.barrier()
+    st = ctx.stats()
+    launches = st.launches * args.steps
+    cap = int(np.maximum(H, 1).sum())
+    tracks = np.zeros(cap, E.TRACK_DTYPE)
+    counts = np.zeros(n, np.uint32)
+    first = np.zeros(n, np.uint64)
+    status = np.zeros(n, np.uint32)
+    ctx.fetch_into(tracks, counts, first, status)
+    T = counts.astype(np.int64)
+    alg_bytes = int((8 + 12 * S + 16 * H).sum() + (4 + 100 * T).sum())
+    ms_max = ranks.max(ms)
+    value = ranks.sum(n) / (ms_max / 1e3)
+
+    # ---- end to end through the C ABI ------------------------------------
+    out_cap = cap
+    h_tracks = ctx.host_alloc(out_cap * 100).view(E.TRACK_DTYPE)
+    h_counts = np.zeros(n, np.uint32)
+    h_first = np.zeros(n, np.uint64)
+    h_status = np.zeros(n, np.uint32)
+    for _ in range(args.warmup):
+        ctx.search_packed_into(hbuf, offs, sizes, opts, h_tracks, h_counts, h_first, h_status)
+    ranks.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.search_packed_into(hbuf, offs, sizes, opts, h_tracks, h_counts, h_first, h_status)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    ranks.barrier()
+    e2e_max = ranks.max(e2e_s)
+    assert np.array_equal(h_counts, counts)
+    h2d = int(total) + 36 * n
+    d2h = 8 + 16 * n + 100 * int(T.sum())
+
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    _, _, _, _, desc = CONFIGS[args.config]
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded VELO events (no public dataset)",
+        "config": {"workload": desc, "events": n, "mean_hits": float(H.mean()), "max_hits": int(H.max()),
+                   "y_lanes": 4, "launch": "persistent" if mode else "per-event",
+                   "threads_per_event": opts.threads_per_event, "smem_bytes_per_cta": st.smem_bytes_per_cta,
+                   "events_in_global_arena": st.events_in_global, "tracks": int(T.sum()),
+                   "l2": "flushed between timed steps (2 x L2 memset); input also larger than L2",
+                   "parallelism": f"weak scaling over {args.gpus} GPU(s), event blocks per rank"},
+        "impl": "gb300",
+        "e2e": {"value": ranks.sum(n) / e2e_max, "unit": "events/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_src,
+                     "note": "algorithmic bytes = input blobs + 4 B count + 100 B per track"},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "status_flags": {"ring_overflow": int(np.sum(status & 1 != 0)),
+                         "track_overflow": int(np.sum(status & 2 != 0))},
+    }
+    if ranks.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(blobs, args.cpu_seconds)
+    ctx.host_free(hbuf)
+    ctx.host_free(h_tracks.view(np.uint8))
+    ctx.close()
+    return line if ranks.rank == 0 else None
+
+
+def main():
+    args = parse_args()
+    ranks = Ranks()
+    try:
+        line = reference_arm(args, ranks) if args.impl == "reference" else gpu_arm(args, ranks)
+        if line is not None and ranks.rank == 0:
+            print(json.dumps(line), flush=True)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,661 @@
+// velo_capi.cpp -- host orchestration behind include/velo_search.h.
+//
+// Replaces invokeParallelSearch (KernelInvoker.cpp:14-275): instead of a fresh
+// OpenCL context, a JIT build and twelve buffers per call, a velo_ctx keeps
+// one CUDA stream and grow-only device buffers; events are validated on the
+// host (headers and module tables), copied with one H2D transfer, searched by
+// one kernel launch, and the tracks come back compacted in one D2H transfer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "velo_internal.h"
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+}  // namespace
+
+struct velo_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  int max_smem_optin = 0;
+  int l2_bytes = 0;
+  std::string err;
+
+  DevBuf d_input, d_ev_offset, d_ev_hits, d_ev_maxmod, d_ev_valid, d_hit_base, d_arena_off, d_order;
+  DevBuf d_tracklets, d_weak, d_tracks, d_out_tracks, d_out_counts, d_out_first, d_out_status;
+  DevBuf d_counters, d_garena, d_flush;
+
+  // staged batch
+  bool staged = false;
+  int32_t n = 0;
+  std::vector<uint64_t> h_offset;
+  std::vector<uint32_t> h_hits, h_maxmod, h_valid;
+  std::vector<uint64_t> h_hit_base;
+  std::vector<uint32_t> h_status;
+  uint64_t rows = 0;
+  uint64_t input_bytes = 0;
+  uint64_t total_hits = 0;
+
+  // per-launch metadata cache
+  bool meta_valid = false;
+  uint32_t meta_smem = 0;
+  int meta_y = 0;
+  int meta_persistent = -1;
+  uint32_t configured_smem = 0;
+  std::vector<uint64_t> h_arena_off;
+  std::vector<int32_t> h_order;
+  int32_t events_in_global = 0;
+
+  void* h_stage = nullptr;
+  size_t h_stage_cap = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  velo_stats stats{};
+  bool ran = false;
+};
+
+namespace {
+
+using velo::ArenaLayout;
+using velo::arena_layout;
+
+velo_status cuda_fail(velo_ctx* c, cudaError_t e, const char* what) {
+  c->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? VELO_ERR_OUT_OF_MEMORY : VELO_ERR_CUDA;
+}
+
+#define VELO_CUDA(c, call)                                   \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return cuda_fail((c), _e, #call); \
+  } while (0)
+
+velo_status ensure(velo_ctx* c, DevBuf& b, size_t bytes, const char* what) {
+  if (bytes == 0) bytes = 16;
+  if (bytes <= b.cap) return VELO_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  const size_t nb = bytes + bytes / 4 + 256;
+  cudaError_t e = cudaMalloc(&b.p, nb);
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  b.cap = nb;
+  return VELO_OK;
+}
+
+template <typename T>
+T* P(DevBuf& b) { return reinterpret_cast<T*>(b.p); }
+
+int32_t rd_i32(const uint8_t* p) {
+  int32_t v;
+  std::memcpy(&v, p, 4);
+  return v;
+}
+
+// Header and module-table checks (coordinates are checked on the device).
+velo_status check_event(const uint8_t* blob, uint64_t size, uint32_t* H_out, uint32_t* M_out) {
+  if (!blob || size < 8) return VELO_ERR_INVALID_EVENT;
+  const int32_t S = rd_i32(blob), H = rd_i32(blob + 4);
+  if (S < 0 || S > VELO_MAX_MODULES || H < 0) return VELO_ERR_INVALID_EVENT;
+  if (size < 8ull + 12ull * (uint64_t)S + 16ull * (uint64_t)H) return VELO_ERR_INVALID_EVENT;
+  int64_t acc = 0;
+  int32_t maxmod = 0;
+  for (int m = 0; m < S; ++m) {
+    const int32_t st = rd_i32(blob + 8 + 4 * (S + m));
+    const int32_t nm = rd_i32(blob + 8 + 4 * (2 * S + m));
+    if (nm < 0 || nm > VELO_MAX_MODULE_HITS || st != acc) return VELO_ERR_INVALID_EVENT;
+    acc += nm;
+    maxmod = std::max(maxmod, nm);
+  }
+  if (acc != H) return VELO_ERR_INVALID_EVENT;
+  if (H_out) *H_out = (uint32_t)H;
+  if (M_out) *M_out = (uint32_t)maxmod;
+  return VELO_OK;
+}
+
+// Reference per-module x-sort: first-element-pivot partition of
+// Tools.cpp:125-157, applied per module over the contiguous hit ranges as
+// preorder_by_x does (Tools.cpp:53-64).  Same permutation for equal keys.
+void swap4(float* a, float* b, float* c, uint32_t* d, int i, int j) {
+  std::swap(a[i], a[j]);
+  std::swap(b[i], b[j]);
+  std::swap(c[i], c[j]);
+  std::swap(d[i], d[j]);
+}
+
+int partition4(float* a, float* b, float* c, uint32_t* d, int lo, int hi) {
+  const float pivot = a[lo];
+  int l = lo, r = hi;
+  while (l < r) {
+    while (a[r] > pivot) r--;
+    while (l < r && a[l] <= pivot) l++;
+    if (l < r) swap4(a, b, c, d, l, r);
+  }
+  swap4(a, b, c, d, r, lo);
+  return r;
+}
+
+void sort_range(float* a, float* b, float* c, uint32_t* d, int lo, int hi) {
+  std::vector<std::pair<int, int>> stack;
+  stack.emplace_back(lo, hi);
+  while (!stack.empty()) {
+    auto [s, e] = stack.back();
+    stack.pop_back();
+    if (s >= e) continue;
+    const int p = partition4(a, b, c, d, s, e);
+    stack.emplace_back(s, p - 1);
+    stack.emplace_back(p + 1, e);
+  }
+}
+
+uint32_t resolve_threads(int32_t t) {
+  if (t == 64 || t == 128 || t == 256 || t == 512) return (uint32_t)t;
+  return 256;
+}
+
+}  // namespace
+
+extern "C" {
+
+void velo_default_options(velo_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->y_lanes = 4;
+  o->threads_per_event = 256;
+  o->launch_mode = VELO_LAUNCH_PER_EVENT;
+  o->smem_hits = 0;
+  o->narrow_windows = 1;
+  o->ctas_per_sm = 0;
+  o->use_graph = 0;
+}
+
+const char* velo_status_string(velo_status s) {
+  switch (s) {
+    case VELO_OK: return "ok";
+    case VELO_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case VELO_ERR_INVALID_EVENT: return "invalid event blob";
+    case VELO_ERR_CAPACITY: return "track buffer too small";
+    case VELO_ERR_CUDA: return "CUDA error";
+    case VELO_ERR_TIMEOUT: return "device wait timed out";
+    case VELO_ERR_NO_DEVICE: return "no CUDA device";
+    case VELO_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case VELO_ERR_NOT_STAGED: return "no staged events";
+  }
+  return "unknown status";
+}
+
+velo_status velo_validate_event(const uint8_t* blob, uint64_t size) {
+  velo_status st = check_event(blob, size, nullptr, nullptr);
+  if (st != VELO_OK) return st;
+  const int32_t S = rd_i32(blob), H = rd_i32(blob + 4);
+  const uint8_t* xyz = blob + 8 + 12ull * S + 4ull * H;
+  for (int64_t i = 0; i < 3ll * H; ++i) {
+    float v;
+    std::memcpy(&v, xyz + 4 * i, 4);
+    if (!std::isfinite(v)) return VELO_ERR_INVALID_EVENT;
+  }
+  return VELO_OK;
+}
+
+velo_status velo_sort_by_x(uint8_t* blob, uint64_t size) {
+  velo_status st = velo_validate_event(blob, size);
+  if (st != VELO_OK) return st;
+  if (reinterpret_cast<uintptr_t>(blob) & 3u) return VELO_ERR_INVALID_ARGUMENT;
+  const int32_t S = rd_i32(blob), H = rd_i32(blob + 4);
+  const int32_t* num = reinterpret_cast<const int32_t*>(blob + 8 + 8ull * S);
+  uint32_t* id = reinterpret_cast<uint32_t*>(blob + 8 + 12ull * S);
+  float* x = reinterpret_cast<float*>(id + H);
+  float* y = x + H;
+  float* z = y + H;
+  int acc = 0;
+  for (int m = 0; m < S; ++m) {
+    sort_range(x, y, z, id, acc, acc + num[m] - 1);
+    acc += num[m];
+  }
+  return VELO_OK;
+}
+
+uint64_t velo_track_capacity(const uint8_t* const* events, const uint64_t* sizes, int32_t n) {
+  uint64_t total = 0;
+  for (int32_t e = 0; e < n; ++e) {
+    int32_t H = 0;
+    if (events && events[e] && sizes && sizes[e] >= 8) H = rd_i32(events[e] + 4);
+    total += H > 0 ? (uint64_t)H : 1ull;
+  }
+  return total;
+}
+
+velo_status velo_create(velo_ctx** out, int32_t device) {
+  if (!out) return VELO_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return VELO_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return VELO_ERR_INVALID_ARGUMENT;
+  velo_ctx* c = new velo_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&c->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->l2_bytes, cudaDevAttrL2CacheSize, device);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->e1);
+  if (e != cudaSuccess) {
+    velo_destroy(c);
+    return VELO_ERR_CUDA;
+  }
+  *out = c;
+  return VELO_OK;
+}
+
+void velo_destroy(velo_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  DevBuf* bufs[] = {&c->d_input, &c->d_ev_offset, &c->d_ev_hits, &c->d_ev_maxmod, &c->d_ev_valid,
+                    &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_weak,
+                    &c->d_tracks, &c->d_out_tracks, &c->d_out_counts, &c->d_out_first,
+                    &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush};
+  for (DevBuf* b : bufs)
+    if (b->p) cudaFree(b->p);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* velo_last_error(const velo_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+int32_t velo_device_sm_count(const velo_ctx* c) { return c ? c->sm_count : 0; }
+
+velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
+                       int32_t n) {
+  if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  c->staged = false;
+  c->meta_valid = false;
+  c->ran = false;
+  c->n = n;
+  c->h_offset.assign(n, 0);
+  c->h_hits.assign(n, 0);
+  c->h_maxmod.assign(n, 0);
+  c->h_valid.assign(n, 0);
+  c->h_hit_base.assign(n, 0);
+  uint64_t lo = ~0ull, hi = 0;
+  for (int32_t e = 0; e < n; ++e) {
+    if (offsets[e] & 3u) {
+      c->err = "event offsets must be 4-byte aligned";
+      return VELO_ERR_INVALID_ARGUMENT;
+    }
+    lo = std::min(lo, offsets[e]);
+    hi = std::max(hi, offsets[e] + sizes[e]);
+  }
+  if (n == 0) lo = hi = 0;
+  if (reinterpret_cast<uintptr_t>(buf + lo) & 3u) {
+    c->err = "event buffer must be 4-byte aligned";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
+  uint64_t rows = 0, hits = 0;
+  for (int32_t e = 0; e < n; ++e) {
+    uint32_t H = 0, M = 0;
+    const bool ok = check_event(buf + offsets[e], sizes[e], &H, &M) == VELO_OK;
+    c->h_valid[e] = ok ? 1u : 0u;
+    c->h_hits[e] = ok ? H : 0u;
+    c->h_maxmod[e] = ok ? M : 0u;
+    c->h_offset[e] = offsets[e] - lo;
+    c->h_hit_base[e] = rows;
+    rows += std::max<uint64_t>(c->h_hits[e], 1ull);
+    hits += c->h_hits[e];
+  }
+  c->rows = rows;
+  c->total_hits = hits;
+  c->input_bytes = hi - lo;
+  velo_status st;
+  if ((st = ensure(c, c->d_input, hi - lo + 16, "input")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_ev_offset, 8ull * n, "offsets")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_ev_hits, 4ull * n, "hits")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_ev_maxmod, 4ull * n, "maxmod")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_ev_valid, 4ull * n, "valid")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_hit_base, 8ull * n, "hit_base")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_tracklets, 12ull * rows, "tracklets")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_weak, 4ull * rows, "weak")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_tracks, sizeof(velo_track) * rows, "tracks")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_out_tracks, sizeof(velo_track) * rows, "out_tracks")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_out_counts, 4ull * n, "counts")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_out_first, 8ull * n, "first")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_out_status, 4ull * n, "status")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_counters, 64, "counters")) != VELO_OK) return st;
+  if (hi > lo)
+    VELO_CUDA(c, cudaMemcpyAsync(c->d_input.p, buf + lo, hi - lo, cudaMemcpyHostToDevice, c->stream));
+  if (n > 0) {
+    VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_offset.p, c->h_offset.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
+    VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_hits.p, c->h_hits.data(), 4ull * n, cudaMemcpyHostToDevice, c->stream));
+    VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_maxmod.p, c->h_maxmod.data(), 4ull * n, cudaMemcpyHostToDevice, c->stream));
+    VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_valid.p, c->h_valid.data(), 4ull * n, cudaMemcpyHostToDevice, c->stream));
+    VELO_CUDA(c, cudaMemcpyAsync(c->d_hit_base.p, c->h_hit_base.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
+  }
+  c->staged = true;
+  return VELO_OK;
+}
+
+namespace {
+
+velo_status prepare_launch(velo_ctx* c, const velo_options& o, uint32_t* smem_out) {
+  const uint32_t Y = (uint32_t)o.y_lanes;
+  // shared-memory arena size: largest event arena up to the budget
+  uint32_t budget;
+  if (o.smem_hits > 0) {
+    budget = arena_layout((uint32_t)o.smem_hits, std::min<uint32_t>((uint32_t)o.smem_hits, VELO_MAX_MODULE_HITS), Y).total;
+  } else {
+    budget = 68u * 1024u;   // three CTAs per SM next to the static shared state
+  }
+  const uint32_t limit = (uint32_t)std::max(0, c->max_smem_optin - 8 * 1024);
+  budget = std::min(budget, limit);
+  uint32_t smem = 16;
+  for (int32_t e = 0; e < c->n; ++e) {
+    if (!c->h_valid[e]) continue;
+    const uint32_t need = arena_layout(c->h_hits[e], c->h_maxmod[e], Y).total;
+    if (need <= budget) smem = std::max(smem, need);
+  }
+  const bool persistent = o.launch_mode == VELO_LAUNCH_PERSISTENT;
+  if (!c->meta_valid || c->meta_smem != smem || c->meta_y != (int)Y || c->meta_persistent != (int)persistent) {
+    c->h_arena_off.assign(c->n, velo::kNoArena);
+    uint64_t goff = 0;
+    int32_t nglob = 0;
+    for (int32_t e = 0; e < c->n; ++e) {
+      if (!c->h_valid[e]) continue;
+      const uint32_t need = arena_layout(c->h_hits[e], c->h_maxmod[e], Y).total;
+      if (need > smem) {
+        c->h_arena_off[e] = goff;
+        goff += (need + 255u) & ~255ull;
+        nglob++;
+      }
+    }
+    velo_status st;
+    if ((st = ensure(c, c->d_arena_off, 8ull * c->n, "arena_off")) != VELO_OK) return st;
+    if ((st = ensure(c, c->d_garena, goff, "global arena")) != VELO_OK) return st;
+    if (c->n > 0)
+      VELO_CUDA(c, cudaMemcpyAsync(c->d_arena_off.p, c->h_arena_off.data(), 8ull * c->n,
+                                   cudaMemcpyHostToDevice, c->stream));
+    if (persistent) {
+      c->h_order.resize(c->n);
+      std::iota(c->h_order.begin(), c->h_order.end(), 0);
+      std::stable_sort(c->h_order.begin(), c->h_order.end(),
+                       [&](int32_t a, int32_t b) { return c->h_hits[a] > c->h_hits[b]; });
+      if ((st = ensure(c, c->d_order, 4ull * c->n, "order")) != VELO_OK) return st;
+      if (c->n > 0)
+        VELO_CUDA(c, cudaMemcpyAsync(c->d_order.p, c->h_order.data(), 4ull * c->n,
+                                     cudaMemcpyHostToDevice, c->stream));
+    }
+    c->events_in_global = nglob;
+    c->meta_valid = true;
+    c->meta_smem = smem;
+    c->meta_y = (int)Y;
+    c->meta_persistent = persistent ? 1 : 0;
+  }
+  if (c->configured_smem < smem) {
+    int e = velo::configure_search_kernel(smem);
+    if (e != 0) return cuda_fail(c, (cudaError_t)e, "cudaFuncSetAttribute");
+    c->configured_smem = smem;
+  }
+  *smem_out = smem;
+  return VELO_OK;
+}
+
+velo_status check_options(velo_ctx* c, const velo_options* opts, velo_options* o) {
+  if (opts) *o = *opts; else velo_default_options(o);
+  if (o->y_lanes < 1 || o->y_lanes > 16) {
+    c->err = "y_lanes must be in 1..16";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
+  if (o->launch_mode != VELO_LAUNCH_PER_EVENT && o->launch_mode != VELO_LAUNCH_PERSISTENT) {
+    c->err = "unknown launch_mode";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
+  o->threads_per_event = (int32_t)resolve_threads(o->threads_per_event);
+  return VELO_OK;
+}
+
+// memset of the queue head / output cursor, then the search kernel.
+velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
+  VELO_CUDA(c, cudaMemsetAsync(c->d_counters.p, 0, 64, c->stream));
+  if (c->n == 0) {
+    c->stats.launches = 0;
+    return VELO_OK;
+  }
+  velo::SearchParams p{};
+  p.input = P<uint8_t>(c->d_input);
+  p.ev_offset = P<uint64_t>(c->d_ev_offset);
+  p.ev_hits = P<uint32_t>(c->d_ev_hits);
+  p.ev_maxmod = P<uint32_t>(c->d_ev_maxmod);
+  p.ev_valid = P<uint32_t>(c->d_ev_valid);
+  p.hit_base = P<uint64_t>(c->d_hit_base);
+  p.arena_off = P<uint64_t>(c->d_arena_off);
+  p.order = P<int32_t>(c->d_order);
+  p.n_events = c->n;
+  p.y_lanes = o.y_lanes;
+  p.narrow = o.narrow_windows ? 1 : 0;
+  p.persistent = o.launch_mode == VELO_LAUNCH_PERSISTENT ? 1 : 0;
+  p.smem_arena_bytes = smem;
+  p.global_arena = P<uint8_t>(c->d_garena);
+  p.tracklets = P<uint32_t>(c->d_tracklets);
+  p.weak = P<uint32_t>(c->d_weak);
+  p.tracks = P<velo_track>(c->d_tracks);
+  p.out_tracks = P<velo_track>(c->d_out_tracks);
+  p.out_counts = P<uint32_t>(c->d_out_counts);
+  p.out_first = P<uint64_t>(c->d_out_first);
+  p.out_status = P<uint32_t>(c->d_out_status);
+  p.out_cursor = P<unsigned long long>(c->d_counters);
+  p.work_counter = reinterpret_cast<int32_t*>(P<uint8_t>(c->d_counters) + 32);
+  const int block = o.threads_per_event;
+  int grid = c->n;
+  if (p.persistent) {
+    int per_sm = o.ctas_per_sm;
+    if (per_sm <= 0) {
+      int occ = 0;
+      int e = velo::search_occupancy(block, smem, &occ);
+      if (e != 0) return cuda_fail(c, (cudaError_t)e, "occupancy");
+      per_sm = std::max(occ, 1);
+    }
+    grid = std::min<int64_t>((int64_t)c->sm_count * per_sm, c->n);
+  }
+  int e = velo::launch_search(p, grid, block, smem, c->stream);
+  if (e != 0) return cuda_fail(c, (cudaError_t)e, "search kernel launch");
+  c->stats.launches = 1;
+  c->stats.grid = grid;
+  c->stats.block = block;
+  c->stats.smem_bytes_per_cta = (int32_t)smem;
+  return VELO_OK;
+}
+
+}  // namespace
+
+velo_status velo_run(velo_ctx* c, const velo_options* opts) {
+  if (!c) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->staged) return VELO_ERR_NOT_STAGED;
+  velo_options o;
+  velo_status st = check_options(c, opts, &o);
+  if (st != VELO_OK) return st;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  uint32_t smem = 0;
+  if ((st = prepare_launch(c, o, &smem)) != VELO_OK) return st;
+  VELO_CUDA(c, cudaEventRecord(c->e0, c->stream));
+  if ((st = enqueue_run(c, o, smem)) != VELO_OK) return st;
+  VELO_CUDA(c, cudaEventRecord(c->e1, c->stream));
+  c->ran = true;
+  c->stats.n_events = (uint32_t)c->n;
+  c->stats.total_hits = c->total_hits;
+  c->stats.input_bytes = c->input_bytes;
+  c->stats.events_in_global = c->events_in_global;
+  return VELO_OK;
+}
+
+velo_status velo_synchronize(velo_ctx* c) {
+  if (!c) return VELO_ERR_INVALID_ARGUMENT;
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  return VELO_OK;
+}
+
+velo_status velo_fetch(velo_ctx* c, velo_track* tracks_out, uint64_t capacity, uint32_t* counts,
+                       uint64_t* first, uint32_t* status) {
+  if (!c) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->ran) return VELO_ERR_NOT_STAGED;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, c->e0, c->e1) == cudaSuccess) c->stats.kernel_ms = ms;
+  unsigned long long total = 0;
+  VELO_CUDA(c, cudaMemcpyAsync(&total, c->d_counters.p, 8, cudaMemcpyDeviceToHost, c->stream));
+  if (c->n > 0) {
+    if (counts)
+      VELO_CUDA(c, cudaMemcpyAsync(counts, c->d_out_counts.p, 4ull * c->n, cudaMemcpyDeviceToHost, c->stream));
+    if (first)
+      VELO_CUDA(c, cudaMemcpyAsync(first, c->d_out_first.p, 8ull * c->n, cudaMemcpyDeviceToHost, c->stream));
+    c->h_status.resize(c->n);
+    VELO_CUDA(c, cudaMemcpyAsync(c->h_status.data(), c->d_out_status.p, 4ull * c->n,
+                                 cudaMemcpyDeviceToHost, c->stream));
+  }
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (status && c->n > 0) std::memcpy(status, c->h_status.data(), 4ull * c->n);
+  c->stats.total_tracks = total;
+  c->stats.output_bytes = 4ull * c->n + sizeof(velo_track) * total;
+  if (tracks_out == nullptr && capacity == 0) return VELO_OK;
+  if (total > capacity) {
+    c->err = "track buffer holds " + std::to_string(capacity) + " tracks, " + std::to_string(total) + " needed";
+    return VELO_ERR_CAPACITY;
+  }
+  if (total > 0)
+    VELO_CUDA(c, cudaMemcpyAsync(tracks_out, c->d_out_tracks.p, sizeof(velo_track) * total,
+                                 cudaMemcpyDeviceToHost, c->stream));
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  return VELO_OK;
+}
+
+velo_status velo_get_stats(const velo_ctx* c, velo_stats* s) {
+  if (!c || !s) return VELO_ERR_INVALID_ARGUMENT;
+  *s = c->stats;
+  return VELO_OK;
+}
+
+velo_status velo_search_packed(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
+                               const uint64_t* sizes, int32_t n, const velo_options* opts,
+                               velo_track* tracks_out, uint64_t capacity, uint32_t* counts,
+                               uint64_t* first, uint32_t* status) {
+  velo_status st = velo_stage(c, buf, offsets, sizes, n);
+  if (st != VELO_OK) return st;
+  if ((st = velo_run(c, opts)) != VELO_OK) return st;
+  st = velo_fetch(c, tracks_out, capacity, counts, first, status);
+  if (st != VELO_OK) return st;
+  for (int32_t e = 0; e < n; ++e)
+    if (c->h_status[e] & VELO_EVENT_INVALID) {
+      c->err = "event " + std::to_string(e) + " failed validation";
+      return VELO_ERR_INVALID_EVENT;
+    }
+  return VELO_OK;
+}
+
+velo_status velo_search(velo_ctx* c, const uint8_t* const* events, const uint64_t* sizes, int32_t n,
+                        const velo_options* opts, velo_track* tracks_out, uint64_t capacity,
+                        uint32_t* counts, uint64_t* first, uint32_t* status) {
+  if (!c || n < 0 || (n > 0 && (!events || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  std::vector<uint64_t> offs(n);
+  uint64_t total = 0;
+  for (int32_t e = 0; e < n; ++e) {
+    offs[e] = total;
+    total += (sizes[e] + 15) & ~15ull;
+  }
+  if (total + 16 > c->h_stage_cap) {
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    c->h_stage_cap = 0;
+    const size_t nb = total + total / 4 + 4096;
+    VELO_CUDA(c, cudaHostAlloc(&c->h_stage, nb, cudaHostAllocDefault));
+    c->h_stage_cap = nb;
+  }
+  uint8_t* stage = static_cast<uint8_t*>(c->h_stage);
+  // pack the events into pinned memory, in parallel for large batches
+  auto pack = [&](int32_t a, int32_t b) {
+    for (int32_t e = a; e < b; ++e)
+      if (events[e] && sizes[e]) std::memcpy(stage + offs[e], events[e], sizes[e]);
+  };
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (total > (64ull << 20) && hw > 1 && n > 64) {
+    std::vector<std::thread> th;
+    const int32_t chunk = (n + (int32_t)hw - 1) / (int32_t)hw;
+    for (unsigned t = 0; t < hw; ++t) {
+      const int32_t a = (int32_t)t * chunk, b = std::min(n, a + chunk);
+      if (a < b) th.emplace_back(pack, a, b);
+    }
+    for (auto& t : th) t.join();
+  } else {
+    pack(0, n);
+  }
+  return velo_search_packed(c, stage, offs.data(), sizes, n, opts, tracks_out, capacity, counts, first,
+                            status);
+}
+
+velo_status velo_time_runs(velo_ctx* c, const velo_options* opts, int32_t warmup, int32_t iters,
+                           int32_t flush_l2, float* ms_out) {
+  if (!c || iters <= 0 || warmup < 0 || !ms_out) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->staged) return VELO_ERR_NOT_STAGED;
+  velo_options o;
+  velo_status st = check_options(c, opts, &o);
+  if (st != VELO_OK) return st;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  uint32_t smem = 0;
+  if ((st = prepare_launch(c, o, &smem)) != VELO_OK) return st;
+  const size_t flush_bytes = (size_t)std::max(c->l2_bytes, 1 << 20) * 2;
+  if (flush_l2 && (st = ensure(c, c->d_flush, flush_bytes, "l2 flush")) != VELO_OK) return st;
+  for (int32_t i = 0; i < warmup; ++i)
+    if ((st = enqueue_run(c, o, smem)) != VELO_OK) return st;
+  double total = 0.0;
+  for (int32_t i = 0; i < iters; ++i) {
+    if (flush_l2) VELO_CUDA(c, cudaMemsetAsync(c->d_flush.p, i & 0xff, flush_bytes, c->stream));
+    VELO_CUDA(c, cudaEventRecord(c->e0, c->stream));
+    if ((st = enqueue_run(c, o, smem)) != VELO_OK) return st;
+    VELO_CUDA(c, cudaEventRecord(c->e1, c->stream));
+    VELO_CUDA(c, cudaEventSynchronize(c->e1));
+    float ms = 0.f;
+    VELO_CUDA(c, cudaEventElapsedTime(&ms, c->e0, c->e1));
+    total += ms;
+  }
+  *ms_out = (float)(total / iters);
+  c->ran = true;
+  c->stats.kernel_ms = *ms_out;
+  c->stats.n_events = (uint32_t)c->n;
+  c->stats.total_hits = c->total_hits;
+  c->stats.input_bytes = c->input_bytes;
+  c->stats.events_in_global = c->events_in_global;
+  return VELO_OK;
+}
+
+velo_status velo_host_alloc(velo_ctx* c, uint64_t bytes, void** ptr) {
+  if (!c || !ptr) return VELO_ERR_INVALID_ARGUMENT;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  VELO_CUDA(c, cudaHostAlloc(ptr, bytes ? bytes : 16, cudaHostAllocDefault));
+  return VELO_OK;
+}
+
+velo_status velo_host_free(velo_ctx* c, void* ptr) {
+  if (!c) return VELO_ERR_INVALID_ARGUMENT;
+  if (ptr) VELO_CUDA(c, cudaFreeHost(ptr));
+  return VELO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,123 @@
+// velo_host.cpp -- the reference's C++ host entry points
+// (GpuPixelSearchByTriplet.cpp:4-65, KernelInvoker.cpp:14-275,
+// Tools.cpp:46-66) on top of the C ABI.
+//
+// One process-wide context on device 0 (or $VELO_DEVICE) serves these calls,
+// created on first use; like the reference (host globals h_*, Tools.cpp:5-13)
+// they are not re-entrant.  The reference's timing sweep over local sizes
+// (KernelInvoker.cpp:138-193: four Y values, four launches each, output kept
+// from Y = 4) is not repeated: one launch with Y = 4 produces that output.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <mutex>
+#include <vector>
+
+#include "../../include/GpuPixelSearchByTriplet.h"
+#include "../../include/velo_search.h"
+
+namespace {
+
+int g_verbosity = 0;   // 3 in standalone mode, 0 in framework mode (GpuPixelSearchByTriplet.cpp:16,35)
+velo_ctx* g_ctx = nullptr;
+std::mutex g_mutex;
+
+[[noreturn]] void fail(const char* where, velo_status st, const char* detail) {
+  std::cerr << "Error in function " << where << std::endl
+            << "Error string: " << velo_status_string(st) << (detail && *detail ? ": " : "")
+            << (detail ? detail : "") << std::endl;
+  std::exit(-1);   // Tools.h:27-34
+}
+
+velo_ctx* context() {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_ctx) {
+    int dev = 0;
+    if (const char* d = std::getenv("VELO_DEVICE")) dev = std::atoi(d);
+    velo_status st = velo_create(&g_ctx, dev);
+    if (st != VELO_OK) fail("velo_create", st, nullptr);
+  }
+  return g_ctx;
+}
+
+}  // namespace
+
+int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
+                         const std::vector<const std::vector<uint8_t>*>& input,
+                         std::vector<std::vector<uint8_t> >& output) {
+  if (eventsToProcess <= 0) return 0;
+  velo_ctx* c = context();
+  std::vector<const uint8_t*> ptrs(eventsToProcess);
+  std::vector<uint64_t> sizes(eventsToProcess);
+  for (int i = 0; i < eventsToProcess; ++i) {
+    const std::vector<uint8_t>* v = input[startingEvent + i];
+    ptrs[i] = v->empty() ? nullptr : v->data();
+    sizes[i] = v->size();
+  }
+  const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), eventsToProcess);
+  std::vector<velo_track> tracks(cap);
+  std::vector<uint32_t> counts(eventsToProcess), status(eventsToProcess);
+  std::vector<uint64_t> first(eventsToProcess);
+  velo_options opts;
+  velo_default_options(&opts);   // Y = 4: the reference's output configuration
+  velo_status st = velo_search(c, ptrs.data(), sizes.data(), eventsToProcess, &opts, tracks.data(), cap,
+                               counts.data(), first.data(), status.data());
+  if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
+  for (int i = 0; i < eventsToProcess; ++i) {
+    std::vector<uint8_t>& out = output[startingEvent + i];
+    out.resize((size_t)counts[i] * sizeof(velo_track));
+    if (counts[i]) std::memcpy(out.data(), &tracks[first[i]], out.size());
+  }
+  if (g_verbosity >= 3) {
+    velo_stats s;
+    velo_get_stats(c, &s);
+    std::cout << "Searched " << eventsToProcess << " events on the GPU: " << s.total_tracks << " tracks, "
+              << s.kernel_ms << " ms" << std::endl;
+  }
+  return 0;
+}
+
+int gpuPixelSearchByTripletInvocation(const std::vector<const std::vector<uint8_t>*>& input,
+                                      std::vector<std::vector<uint8_t> >& output) {
+  if (g_verbosity >= 3)
+    std::cout << "Invoking gpuPixelSearchByTriplet with " << input.size() << " events" << std::endl;
+  output.resize(input.size());
+  const int max_events_to_process_per_kernel = 16000;   // GpuPixelSearchByTriplet.cpp:53
+  for (size_t i = 0; i < input.size(); i += max_events_to_process_per_kernel) {
+    int n = (int)(input.size() - i);
+    if (n > max_events_to_process_per_kernel) n = max_events_to_process_per_kernel;
+    invokeParallelSearch((int)i, n, input, output);
+  }
+  return 0;
+}
+
+void preorder_by_x(std::vector<const std::vector<uint8_t>*>& input) {
+  for (const std::vector<uint8_t>* ev : input) {
+    if (!ev || ev->empty()) continue;
+    // The reference sorts the caller's buffers in place through const
+    // pointers (Tools.cpp:51-63); so does this.
+    uint8_t* blob = const_cast<uint8_t*>(ev->data());
+    velo_status st = velo_sort_by_x(blob, ev->size());
+    if (st != VELO_OK) fail("preorder_by_x", st, nullptr);
+  }
+}
+
+int independent_execute(const std::vector<std::vector<uint8_t> >& input,
+                        std::vector<std::vector<uint8_t> >& output) {
+  std::vector<const std::vector<uint8_t>*> converted(input.size());
+  for (size_t i = 0; i < input.size(); ++i) converted[i] = &input[i];
+  g_verbosity = 3;
+  preorder_by_x(converted);
+  return gpuPixelSearchByTripletInvocation(converted, output);
+}
+
+void independent_post_execute(const std::vector<std::vector<uint8_t> >& output) {
+  if (g_verbosity >= 3) std::cout << std::endl << "Size of output: " << output.size() << " entries" << std::endl;
+}
+
+int gpuPixelSearchByTriplet(const std::vector<const std::vector<uint8_t>*>& input,
+                            std::vector<std::vector<uint8_t> >& output) {
+  g_verbosity = 0;
+  return gpuPixelSearchByTripletInvocation(input, output);
+}

@@ -1,0 +1,254 @@
+"""ctypes binding of ``libclforward_gb300.so`` (the C ABI in include/velo_search.h).
+
+The library is the only compute path: if it has not been built, or no CUDA
+device is present, the calls that need it raise; there is no CPU fallback.
+Host-only helpers (validation, the reference x-sort) work without a GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .events import TRACK_DTYPE
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libclforward_gb300.so")
+
+# velo_status
+OK = 0
+ERR_INVALID_ARGUMENT = -1
+ERR_INVALID_EVENT = -2
+ERR_CAPACITY = -3
+ERR_CUDA = -4
+ERR_TIMEOUT = -5
+ERR_NO_DEVICE = -6
+ERR_OUT_OF_MEMORY = -7
+ERR_NOT_STAGED = -8
+
+# per-event status bits
+EVENT_RING_OVERFLOW = 0x1
+EVENT_TRACK_OVERFLOW = 0x2
+EVENT_MAX_TRACKS = 0x4
+EVENT_INVALID = 0x8
+EVENT_DEGENERATE = 0x10
+
+LAUNCH_PER_EVENT = 0
+LAUNCH_PERSISTENT = 1
+
+# every symbol include/velo_search.h declares
+EXPORTED = [
+    "velo_default_options", "velo_status_string", "velo_create", "velo_destroy", "velo_last_error",
+    "velo_validate_event", "velo_sort_by_x", "velo_track_capacity", "velo_search",
+    "velo_search_packed", "velo_stage", "velo_run", "velo_fetch", "velo_synchronize",
+    "velo_get_stats", "velo_time_runs", "velo_host_alloc", "velo_host_free", "velo_device_sm_count",
+]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("y_lanes", ctypes.c_int32), ("threads_per_event", ctypes.c_int32),
+                ("launch_mode", ctypes.c_int32), ("smem_hits", ctypes.c_int32),
+                ("narrow_windows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32 * 9)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("kernel_ms", ctypes.c_float), ("launches", ctypes.c_uint32),
+                ("n_events", ctypes.c_uint32), ("total_hits", ctypes.c_uint64),
+                ("total_tracks", ctypes.c_uint64), ("input_bytes", ctypes.c_uint64),
+                ("output_bytes", ctypes.c_uint64), ("smem_bytes_per_cta", ctypes.c_int32),
+                ("grid", ctypes.c_int32), ("block", ctypes.c_int32),
+                ("events_in_global", ctypes.c_int32)]
+
+
+class VeloError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Load the native library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"native library missing: {LIB_PATH}; run cl_forward_gb300.build.build()")
+    l = ctypes.CDLL(LIB_PATH)
+    vp, i32, u64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint64
+    l.velo_default_options.argtypes = [ctypes.POINTER(Options)]
+    l.velo_default_options.restype = None
+    l.velo_status_string.argtypes = [ctypes.c_int]
+    l.velo_status_string.restype = ctypes.c_char_p
+    l.velo_create.argtypes = [ctypes.POINTER(vp), i32]
+    l.velo_destroy.argtypes = [vp]
+    l.velo_destroy.restype = None
+    l.velo_last_error.argtypes = [vp]
+    l.velo_last_error.restype = ctypes.c_char_p
+    l.velo_validate_event.argtypes = [vp, u64]
+    l.velo_sort_by_x.argtypes = [vp, u64]
+    l.velo_track_capacity.argtypes = [vp, vp, i32]
+    l.velo_track_capacity.restype = u64
+    l.velo_search.argtypes = [vp, vp, vp, i32, ctypes.POINTER(Options), vp, u64, vp, vp, vp]
+    l.velo_search_packed.argtypes = [vp, vp, vp, vp, i32, ctypes.POINTER(Options), vp, u64, vp, vp, vp]
+    l.velo_stage.argtypes = [vp, vp, vp, vp, i32]
+    l.velo_run.argtypes = [vp, ctypes.POINTER(Options)]
+    l.velo_fetch.argtypes = [vp, vp, u64, vp, vp, vp]
+    l.velo_synchronize.argtypes = [vp]
+    l.velo_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    l.velo_time_runs.argtypes = [vp, ctypes.POINTER(Options), i32, i32, i32, ctypes.POINTER(ctypes.c_float)]
+    l.velo_host_alloc.argtypes = [vp, u64, ctypes.POINTER(vp)]
+    l.velo_host_free.argtypes = [vp, vp]
+    l.velo_device_sm_count.argtypes = [vp]
+    l.velo_device_sm_count.restype = i32
+    _lib = l
+    return l
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    load().velo_default_options(ctypes.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, int(v))
+    return o
+
+
+def validate_event(blob: bytes) -> int:
+    buf = np.frombuffer(blob, np.uint8)
+    return int(load().velo_validate_event(_p(buf) if len(buf) else None, len(blob)))
+
+
+def sort_by_x(blob: bytes) -> bytes:
+    """The reference's per-module x-sort (Tools.cpp:46-66) of one event blob."""
+    buf = np.frombuffer(bytearray(blob), np.uint8).copy()
+    st = load().velo_sort_by_x(_p(buf), len(blob))
+    if st != OK:
+        raise VeloError(st, "velo_sort_by_x")
+    return buf.tobytes()
+
+
+class Context:
+    """One CUDA stream and its device buffers (``velo_ctx``)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        self._h = ctypes.c_void_p()
+        st = self._lib.velo_create(ctypes.byref(self._h), device)
+        if st != OK:
+            raise VeloError(st, f"velo_create: {self._lib.velo_status_string(st).decode()}")
+
+    def close(self):
+        if self._h:
+            self._lib.velo_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int, what: str):
+        if st != OK:
+            detail = self._lib.velo_last_error(self._h).decode(errors="replace")
+            raise VeloError(st, f"{what}: {self._lib.velo_status_string(st).decode()}: {detail}")
+
+    @property
+    def sm_count(self) -> int:
+        return int(self._lib.velo_device_sm_count(self._h))
+
+    # -- one-call host path ------------------------------------------------
+    def search(self, blobs: Sequence[bytes], options: Optional[Options] = None, allow_invalid: bool = False):
+        """Search x-sorted events.  Returns (list of per-event Track arrays, status uint32[n])."""
+        n = len(blobs)
+        arrs = [np.frombuffer(b, np.uint8) for b in blobs]
+        ptrs = (ctypes.c_void_p * max(n, 1))(*[a.ctypes.data if len(a) else 0 for a in arrs])
+        sizes = np.array([len(b) for b in blobs], np.uint64)
+        cap = int(self._lib.velo_track_capacity(ptrs, _p(sizes), n))
+        tracks = np.zeros(max(cap, 1), TRACK_DTYPE)
+        counts = np.zeros(max(n, 1), np.uint32)
+        first = np.zeros(max(n, 1), np.uint64)
+        status = np.zeros(max(n, 1), np.uint32)
+        opts = options or default_options()
+        st = self._lib.velo_search(self._h, ptrs, _p(sizes), n, ctypes.byref(opts), _p(tracks), cap,
+                                   _p(counts), _p(first), _p(status))
+        if not (allow_invalid and st == ERR_INVALID_EVENT):
+            self._check(st, "velo_search")
+        out = [tracks[int(first[e]):int(first[e]) + int(counts[e])].copy() for e in range(n)]
+        return out, status[:n].copy()
+
+    # -- split path ----------------------------------------------------------
+    def stage(self, buf: np.ndarray, offsets: np.ndarray, sizes: np.ndarray):
+        self._staged = (buf, offsets, sizes)   # keep host memory alive until the copy is done
+        self._check(self._lib.velo_stage(self._h, buf.ctypes.data, _p(offsets), _p(sizes), len(offsets)),
+                    "velo_stage")
+
+    def run(self, options: Optional[Options] = None):
+        opts = options or default_options()
+        self._check(self._lib.velo_run(self._h, ctypes.byref(opts)), "velo_run")
+
+    def fetch(self, n_events: int, capacity: int):
+        tracks = np.zeros(max(capacity, 1), TRACK_DTYPE)
+        counts = np.zeros(max(n_events, 1), np.uint32)
+        first = np.zeros(max(n_events, 1), np.uint64)
+        status = np.zeros(max(n_events, 1), np.uint32)
+        self._check(self._lib.velo_fetch(self._h, _p(tracks), capacity, _p(counts), _p(first), _p(status)),
+                    "velo_fetch")
+        return tracks, counts[:n_events], first[:n_events], status[:n_events]
+
+    def fetch_into(self, tracks: np.ndarray, counts: np.ndarray, first: np.ndarray, status: np.ndarray):
+        self._check(self._lib.velo_fetch(self._h, _p(tracks), len(tracks), _p(counts), _p(first),
+                                         _p(status)), "velo_fetch")
+
+    def search_packed_into(self, buf, offsets, sizes, options, tracks, counts, first, status):
+        st = self._lib.velo_search_packed(self._h, buf.ctypes.data, _p(offsets), _p(sizes), len(offsets),
+                                          ctypes.byref(options), _p(tracks), len(tracks), _p(counts),
+                                          _p(first), _p(status))
+        self._check(st, "velo_search_packed")
+
+    def time_runs(self, options: Optional[Options] = None, warmup: int = 3, iters: int = 10,
+                  flush_l2: bool = True) -> float:
+        opts = options or default_options()
+        ms = ctypes.c_float()
+        self._check(self._lib.velo_time_runs(self._h, ctypes.byref(opts), warmup, iters, int(flush_l2),
+                                             ctypes.byref(ms)), "velo_time_runs")
+        return float(ms.value)
+
+    def stats(self) -> Stats:
+        s = Stats()
+        self._check(self._lib.velo_get_stats(self._h, ctypes.byref(s)), "velo_get_stats")
+        return s
+
+    def synchronize(self):
+        self._check(self._lib.velo_synchronize(self._h), "velo_synchronize")
+
+    def host_alloc(self, nbytes: int) -> np.ndarray:
+        """Pinned host buffer (uint8 array); freed by :meth:`host_free`."""
+        p = ctypes.c_void_p()
+        self._check(self._lib.velo_host_alloc(self._h, nbytes, ctypes.byref(p)), "velo_host_alloc")
+        arr = np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p.value))
+        return arr
+
+    def host_free(self, arr: np.ndarray):
+        self._check(self._lib.velo_host_free(self._h, ctypes.c_void_p(arr.ctypes.data)), "velo_host_free")

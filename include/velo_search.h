@@ -1,0 +1,163 @@
+/*
+ * velo_search.h -- C ABI of the GB300 (sm_103a) search-by-triplet VELO track
+ * reconstruction.
+ *
+ * It replaces the OpenCL device layer of dcampora/cl_forward:
+ * invokeParallelSearch (KernelInvoker.h:27-31, KernelInvoker.cpp:14-275) and
+ * the kernel it launches, clSearchByTriplets (Kernel.cl:597-816).  The
+ * reference's C++ entry points keep their signatures in
+ * GpuPixelSearchByTriplet.h and are implemented on top of this ABI.
+ *
+ * Input: per event, one blob in the layout of setHPointersFromInput
+ * (Tools.cpp:68-80):
+ *     int32 S, H; int32 sensor_Zs[S], sensor_hitStarts[S], sensor_hitNums[S];
+ *     uint32 hit_IDs[H]; float32 hit_Xs[H], hit_Ys[H], hit_Zs[H]
+ * with each module's hits x-sorted (velo_sort_by_x applies the reference's
+ * preorder_by_x, Tools.cpp:46-66).
+ * Output: per event, velo_track records (bit-identical to the reference's
+ * Track, KernelDefinitions.h:59-62) whose hits are event-local indices into
+ * the x-sorted hit arrays.
+ *
+ * All entry points are plain C: pointers, sizes and status codes.  A context
+ * owns one CUDA stream and its device buffers; use one context per host
+ * thread.  Nothing here is re-entrant on the same context.
+ */
+#ifndef VELO_SEARCH_H
+#define VELO_SEARCH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VELO_MAX_TRACK_SIZE 24      /* KernelDefinitions.h:16 */
+#define VELO_MAX_TRACKS 3000        /* KernelDefinitions.h:15 */
+#define VELO_TTF_MODULO 2000        /* KernelDefinitions.h:23 */
+#define VELO_MAX_MODULES 255        /* this implementation's limit on S */
+#define VELO_MAX_MODULE_HITS 16383  /* this implementation's limit on hits per module */
+
+/* Track {uint hitsNum; uint hits[24];}: 100 bytes, KernelDefinitions.h:59-62 */
+typedef struct velo_track {
+  uint32_t hitsNum;
+  uint32_t hits[VELO_MAX_TRACK_SIZE];
+} velo_track;
+
+typedef enum velo_status {
+  VELO_OK = 0,
+  VELO_ERR_INVALID_ARGUMENT = -1,
+  VELO_ERR_INVALID_EVENT = -2,     /* an event blob failed validation (see event status) */
+  VELO_ERR_CAPACITY = -3,          /* caller's track buffer too small; counts are valid */
+  VELO_ERR_CUDA = -4,              /* CUDA runtime error; see velo_last_error */
+  VELO_ERR_TIMEOUT = -5,           /* a device-side wait gave up (no GPU hang) */
+  VELO_ERR_NO_DEVICE = -6,
+  VELO_ERR_OUT_OF_MEMORY = -7,
+  VELO_ERR_NOT_STAGED = -8         /* velo_run/velo_fetch without staged input */
+} velo_status;
+
+/* Per-event status bits (event_status_out).  Bits 0x1, 0x2, 0x4 and 0x10 mark
+ * events on which the reference itself has undefined or schedule-dependent
+ * behaviour; results there are this implementation's (it never overruns). */
+#define VELO_EVENT_RING_OVERFLOW 0x1u   /* > TTF_MODULO ring entries in flight (Kernel.cl:344,354,565) */
+#define VELO_EVENT_TRACK_OVERFLOW 0x2u  /* a track needed a 25th hit (Kernel.cl:321) */
+#define VELO_EVENT_MAX_TRACKS 0x4u      /* more than MAX_TRACKS tracks (Kernel.cl:336,810) */
+#define VELO_EVENT_INVALID 0x8u         /* blob failed validation; no tracks */
+#define VELO_EVENT_DEGENERATE 0x10u     /* an inf/NaN fit (two modules' hits at equal z) */
+
+typedef enum velo_launch_mode {
+  VELO_LAUNCH_PER_EVENT = 0,   /* one CTA per event (the reference's one work-group per event) */
+  VELO_LAUNCH_PERSISTENT = 1   /* persistent CTAs pulling events, largest first, from a work queue */
+} velo_launch_mode;
+
+typedef struct velo_options {
+  int32_t y_lanes;            /* reference local size dim 1 (1..16); its output uses 4 */
+  int32_t threads_per_event;  /* 64, 128, 256 or 512 */
+  int32_t launch_mode;        /* velo_launch_mode */
+  int32_t smem_hits;          /* largest event (hits) staged in shared memory; 0 = auto */
+  int32_t narrow_windows;     /* 1: binary-search narrowing of x windows (decisions unchanged) */
+  int32_t ctas_per_sm;        /* persistent mode: resident CTAs per SM; 0 = auto */
+  int32_t use_graph;          /* 1: capture the launch sequence in a CUDA graph and replay it */
+  int32_t reserved[9];
+} velo_options;
+
+typedef struct velo_stats {
+  float kernel_ms;            /* device time of the last velo_run (CUDA events) */
+  uint32_t launches;          /* kernels launched by the last velo_run */
+  uint32_t n_events;
+  uint64_t total_hits;
+  uint64_t total_tracks;
+  uint64_t input_bytes;       /* event blob bytes staged */
+  uint64_t output_bytes;      /* 4 B count + 100 B per track */
+  int32_t smem_bytes_per_cta;
+  int32_t grid;
+  int32_t block;
+  int32_t events_in_global;   /* events too large for the shared-memory arena */
+} velo_stats;
+
+typedef struct velo_ctx velo_ctx;
+
+void velo_default_options(velo_options* opts);
+const char* velo_status_string(velo_status s);
+
+/* Create a context on CUDA device `device`. */
+velo_status velo_create(velo_ctx** ctx, int32_t device);
+void velo_destroy(velo_ctx* ctx);
+const char* velo_last_error(const velo_ctx* ctx);
+
+/* Host-only helpers (no GPU needed). */
+velo_status velo_validate_event(const uint8_t* blob, uint64_t size);
+/* preorder_by_x (Tools.cpp:46-66) of one event, in place; same permutation
+ * as the reference's quicksort, equal x values included. */
+velo_status velo_sort_by_x(uint8_t* blob, uint64_t size);
+/* Upper bound on the tracks n events can produce (sum of max(H, 1)). */
+uint64_t velo_track_capacity(const uint8_t* const* events, const uint64_t* sizes, int32_t n_events);
+
+/*
+ * One call, host buffers in and out (replaces invokeParallelSearch).
+ * Event e's tracks are tracks_out[first_out[e] .. first_out[e] + counts_out[e]).
+ * track_capacity is the room in tracks_out; velo_track_capacity() is always
+ * enough.  event_status_out gets the VELO_EVENT_* bits.
+ */
+velo_status velo_search(velo_ctx* ctx, const uint8_t* const* events, const uint64_t* sizes,
+                        int32_t n_events, const velo_options* opts, velo_track* tracks_out,
+                        uint64_t track_capacity, uint32_t* counts_out, uint64_t* first_out,
+                        uint32_t* event_status_out);
+
+/* Same, for events already packed in one host buffer (event e at
+ * buf + offsets[e], 4-byte aligned).  A pinned buffer is copied directly. */
+velo_status velo_search_packed(velo_ctx* ctx, const uint8_t* buf, const uint64_t* offsets,
+                               const uint64_t* sizes, int32_t n_events, const velo_options* opts,
+                               velo_track* tracks_out, uint64_t track_capacity,
+                               uint32_t* counts_out, uint64_t* first_out,
+                               uint32_t* event_status_out);
+
+/* Split form, for device-resident pipelines and timing:
+ *   velo_stage  validates and copies the events into device memory;
+ *   velo_run    launches the search on the staged events (asynchronous);
+ *   velo_fetch  waits and copies the results of the last run to the host. */
+velo_status velo_stage(velo_ctx* ctx, const uint8_t* buf, const uint64_t* offsets,
+                       const uint64_t* sizes, int32_t n_events);
+velo_status velo_run(velo_ctx* ctx, const velo_options* opts);
+velo_status velo_fetch(velo_ctx* ctx, velo_track* tracks_out, uint64_t track_capacity,
+                       uint32_t* counts_out, uint64_t* first_out, uint32_t* event_status_out);
+velo_status velo_synchronize(velo_ctx* ctx);
+velo_status velo_get_stats(const velo_ctx* ctx, velo_stats* stats);
+
+/* `iters` back-to-back velo_run calls on the staged events, timed with CUDA
+ * events on the context's stream after `warmup` untimed runs.  Between timed
+ * runs a buffer larger than L2 is rewritten when flush_l2 != 0.
+ * ms_out receives the mean device milliseconds per run. */
+velo_status velo_time_runs(velo_ctx* ctx, const velo_options* opts, int32_t warmup, int32_t iters,
+                           int32_t flush_l2, float* ms_out);
+
+/* Pinned host memory (cudaHostAlloc), for callers without a CUDA runtime. */
+velo_status velo_host_alloc(velo_ctx* ctx, uint64_t bytes, void** ptr);
+velo_status velo_host_free(velo_ctx* ctx, void* ptr);
+
+/* Number of streaming multiprocessors of the context's device. */
+int32_t velo_device_sm_count(const velo_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

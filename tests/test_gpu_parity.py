@@ -1,0 +1,168 @@
+"""Parity of the sm_103a search with the reference, through the C ABI.
+
+Golden vectors are the reference kernel's own outputs; everything else is
+compared against the oracle restatement (pinned to the reference by
+test_golden_oracle.py / test_oracle_vs_reference.py) on the same seeded
+events.  Results are integer hit-index lists: the bar is exact equality of
+the per-event track multisets.  Events on which the reference itself is
+undefined (ring / track-size / track-count overflow) are excluded from
+equality and checked for matching status bits instead.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_SETS, GOLDEN_Y, index_lists, index_lists_words
+
+pytestmark = pytest.mark.gpu
+
+OVERFLOW_BITS = 0x1 | 0x2 | 0x4
+
+
+def _sorted(oracle_lib, blobs):
+    return [oracle_lib.sort_by_x(b) for b in blobs]
+
+
+def _assert_same(gpu_ctx, oracle_lib, blobs, y=4, **opts):
+    from cl_forward_gb300 import native
+    got, gst = gpu_ctx.search(blobs, native.default_options(y_lanes=y, **opts))
+    want, ost = oracle_lib.search(blobs, y)
+    assert np.array_equal(gst & OVERFLOW_BITS, ost & OVERFLOW_BITS)
+    checked = 0
+    for e in range(len(blobs)):
+        if ost[e] & oracle_lib.PARITY_EXCLUDING:
+            continue
+        assert index_lists(got[e]) == index_lists(want[e]), f"event {e} differs (opts {opts}, Y={y})"
+        checked += 1
+    return got, checked
+
+
+@pytest.mark.parametrize("name", GOLDEN_SETS)
+@pytest.mark.parametrize("y", GOLDEN_Y)
+def test_golden_vectors(gpu_ctx, golden, name, y):
+    from cl_forward_gb300 import native
+    got, status = gpu_ctx.search(golden[name]["sorted"], native.default_options(y_lanes=y))
+    assert not np.any(status)
+    for e, ref in enumerate(golden[name]["tracks"][y]):
+        assert index_lists(got[e]) == index_lists_words(ref), f"{name} event {e}"
+        # whole 100-byte records, zero beyond hitsNum, as the reference writes them
+        words = got[e].view(np.uint32).reshape(-1, 25)
+        assert sorted(map(tuple, words.tolist())) == sorted(map(tuple, ref.tolist()))
+
+
+def test_config_small_100_events(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import generator
+    blobs = _sorted(oracle_lib, generator.generate(range(100))[0])
+    _, n = _assert_same(gpu_ctx, oracle_lib, blobs)
+    assert n == 100
+
+
+@pytest.mark.parametrize("y", [1, 2, 3, 4, 16])
+def test_fuzz_ties_and_lanes(gpu_ctx, oracle_lib, y):
+    from cl_forward_gb300 import fuzz
+    blobs = [fuzz.fuzz_event(5000 + s, max_per_module=20, grid=1.0, lines=10, x_span=45) for s in range(150)]
+    blobs += [fuzz.fuzz_event(2000 + s, jitter_z=True) for s in range(50)]
+    blobs += [fuzz.fuzz_event(s, grid=2.0) for s in range(50)]
+    blobs += [fuzz.fuzz_event(3000 + s, n_modules=3 + s % 20) for s in range(40)]
+    _, n = _assert_same(gpu_ctx, oracle_lib, _sorted(oracle_lib, blobs), y=y)
+    assert n > 200
+
+
+@pytest.mark.parametrize("threads", [64, 128, 256, 512])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_launch_shapes(gpu_ctx, oracle_lib, threads, mode):
+    from cl_forward_gb300 import generator
+    blobs = _sorted(oracle_lib, generator.generate(range(500, 540))[0])
+    _assert_same(gpu_ctx, oracle_lib, blobs, threads_per_event=threads, launch_mode=mode)
+
+
+@pytest.mark.parametrize("narrow", [0, 1])
+@pytest.mark.parametrize("smem_hits", [0, 200])
+def test_narrowing_and_global_arena(gpu_ctx, oracle_lib, narrow, smem_hits):
+    """smem_hits=200 sends most events to the global-memory arena."""
+    from cl_forward_gb300 import fuzz, generator
+    blobs = generator.generate(range(600, 630))[0]
+    blobs += [fuzz.fuzz_event(2100 + s, jitter_z=True) for s in range(20)]
+    blobs = _sorted(oracle_lib, blobs)
+    _assert_same(gpu_ctx, oracle_lib, blobs, narrow_windows=narrow, smem_hits=smem_hits)
+    assert smem_hits == 0 or gpu_ctx.stats().events_in_global > 0
+
+
+def test_unsorted_input_takes_exact_scans(gpu_ctx, oracle_lib):
+    """Without the x-sort the reference's window scans still define the output."""
+    from cl_forward_gb300 import generator
+    blobs = generator.generate(range(700, 720))[0]            # file order, not sorted
+    _assert_same(gpu_ctx, oracle_lib, blobs)
+
+
+def test_dense_and_uneven_events(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import generator
+    blobs = generator.generate(range(100), generator.CONFIG_STRESS)[0]
+    blobs += generator.generate(range(200), generator.CONFIG_BATCHED)[0]
+    blobs = _sorted(oracle_lib, blobs)
+    for mode in (0, 1):
+        _, n = _assert_same(gpu_ctx, oracle_lib, blobs, launch_mode=mode)
+        assert n > 250
+
+
+def test_config_scale_10000_events(gpu_ctx, oracle_lib):
+    """10,000 events (seeds 1000..10999): set parity and identical tracking rates."""
+    from cl_forward_gb300 import generator, native, validation
+    raw, truths = generator.generate_parallel(range(1000, 11000))
+    blobs = _sorted(oracle_lib, raw)
+    got, gst = gpu_ctx.search(blobs, native.default_options())
+    want, ost = oracle_lib.search(blobs, 4)
+    assert np.array_equal(gst & OVERFLOW_BITS, ost & OVERFLOW_BITS)
+    keep = [e for e in range(len(blobs)) if not (ost[e] & oracle_lib.PARITY_EXCLUDING)]
+    assert len(keep) > 9900
+    bad = [e for e in keep if index_lists(got[e]) != index_lists(want[e])]
+    assert not bad, bad[:10]
+    rg = validation.rates(got, blobs, truths)
+    ro = validation.rates(want, blobs, truths)
+    assert abs(rg.efficiency - ro.efficiency) <= 1e-3
+    assert abs(rg.ghost_rate - ro.ghost_rate) <= 1e-3
+    assert abs(rg.clone_rate - ro.clone_rate) <= 1e-3
+
+
+def test_edge_cases(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import events, fuzz, generator, native
+    good = _sorted(oracle_lib, generator.generate(range(3))[0])
+    ev = events.unpack_event(good[1])
+    ev.y[5] = np.inf
+    nonfinite = events.pack_event(ev)
+    batch = [good[0], fuzz.empty_event(), nonfinite, b"\x05\x00\x00\x00", fuzz.empty_event(0), good[2]]
+    got, status = gpu_ctx.search(batch, allow_invalid=True)
+    assert status[2] & native.EVENT_INVALID and status[3] & native.EVENT_INVALID
+    assert len(got[1]) == 0 and len(got[2]) == 0 and len(got[3]) == 0 and len(got[4]) == 0
+    want, _ = oracle_lib.search([good[0], good[2]], 4)
+    assert index_lists(got[0]) == index_lists(want[0])
+    assert index_lists(got[5]) == index_lists(want[1])
+    with pytest.raises(native.VeloError):
+        gpu_ctx.search(batch)                                  # strict call reports the bad events
+    out, st = gpu_ctx.search([])
+    assert out == [] and len(st) == 0
+
+
+def test_context_reuse_is_stable(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import generator
+    small = _sorted(oracle_lib, generator.generate(range(800, 805))[0])
+    big = _sorted(oracle_lib, generator.generate(range(810, 900))[0])
+    a, _ = gpu_ctx.search(small)
+    gpu_ctx.search(big)
+    b, _ = gpu_ctx.search(small)
+    assert [index_lists(x) for x in a] == [index_lists(x) for x in b]
+
+
+def test_split_stage_run_fetch(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import events, generator, native
+    blobs = _sorted(oracle_lib, generator.generate(range(900, 930))[0])
+    buf, offs, sizes = events.pack_events(blobs)
+    gpu_ctx.stage(buf, offs, sizes)
+    gpu_ctx.run(native.default_options(launch_mode=1))
+    cap = int(sum(max(int(np.frombuffer(b[4:8], "<i4")[0]), 1) for b in blobs))
+    tracks, counts, first, status = gpu_ctx.fetch(len(blobs), cap)
+    want, _ = oracle_lib.search(blobs, 4)
+    for e in range(len(blobs)):
+        assert index_lists(tracks[int(first[e]):int(first[e]) + int(counts[e])]) == index_lists(want[e])
+    s = gpu_ctx.stats()
+    assert s.launches == 1 and s.n_events == len(blobs) and s.total_tracks == counts.sum()
+    assert gpu_ctx.time_runs(native.default_options(), warmup=1, iters=2, flush_l2=True) > 0

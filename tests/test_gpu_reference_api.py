@@ -1,0 +1,66 @@
+"""The reference-signature entry points (Python mirror and C++ driver) on the GPU."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import index_lists
+
+pytestmark = pytest.mark.gpu
+
+
+def test_python_mirror_independent_execute(native_lib, oracle_lib):
+    from cl_forward_gb300 import generator, search
+    raw = generator.generate(range(40, 60))[0]
+    inp = [bytearray(b) for b in raw]
+    out = []
+    assert search.independent_execute(inp, out) == 0
+    assert len(out) == len(raw)
+    sorted_blobs = [oracle_lib.sort_by_x(b) for b in raw]
+    assert [bytes(b) for b in inp] == sorted_blobs            # sorted in place, like the reference
+    want, _ = oracle_lib.search(sorted_blobs, 4)
+    for e in range(len(raw)):
+        assert len(out[e]) % 100 == 0
+        assert index_lists(search.tracks_of(out[e])) == index_lists(want[e])
+    out2 = []
+    search.gpuPixelSearchByTriplet(sorted_blobs, out2)
+    assert out2 == out or all(index_lists(search.tracks_of(a)) == index_lists(search.tracks_of(b))
+                              for a, b in zip(out, out2))
+
+
+def test_invoke_parallel_search_window(native_lib, oracle_lib):
+    from cl_forward_gb300 import generator, search
+    blobs = [oracle_lib.sort_by_x(b) for b in generator.generate(range(60, 70))[0]]
+    out = [b"untouched"] * len(blobs)
+    search.invokeParallelSearch(3, 4, blobs, out)
+    assert out[:3] == [b"untouched"] * 3 and out[7:] == [b"untouched"] * 3
+    want, _ = oracle_lib.search(blobs[3:7], 4)
+    for i in range(4):
+        assert index_lists(search.tracks_of(out[3 + i])) == index_lists(want[i])
+
+
+def test_cpp_driver_dump(native_lib, oracle_lib, tmp_path):
+    from cl_forward_gb300 import build, events, generator
+    raw = generator.generate(range(70, 73))[0]
+    data = tmp_path / "data"
+    dump = tmp_path / "dump"
+    data.mkdir()
+    dump.mkdir()
+    for i, b in enumerate(raw):
+        events.write_dat(str(data / f"{i}.dat"), b)
+    r = subprocess.run([build.DRIVER, str(data), "3", "--dump", str(dump)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "3 files read" in r.stdout
+    want, _ = oracle_lib.search([oracle_lib.sort_by_x(b) for b in raw], 4)
+    for i in range(3):
+        text = (dump / f"{i}.out").read_text()
+        tracks = re.findall(r"Track #(\d+), length (\d+)\n(.*?)\n\n", text, re.S)
+        assert len(tracks) == len(want[i])
+        ids = sorted(tuple(sorted(int(m) for m in re.findall(r"^\s+(\d+) \(", body, re.M)))
+                     for _, _, body in tracks)
+        ev = events.unpack_event(oracle_lib.sort_by_x(raw[i]))
+        ref_ids = sorted(tuple(sorted(int(ev.hit_id[h]) for h in t)) for t in index_lists(want[i]))
+        assert ids == ref_ids
