@@ -280,8 +280,13 @@ def gpu_arm(args, ranks: Ranks):
     ctx.stage(hbuf, offs, sizes)
     ctx.synchronize()
     ranks.barrier()
+    for _ in range(args.warmup):
+        ctx.run(opts)
+    ctx.synchronize()
     with Clocks(ranks.local) as clk:
-        ms = ctx.time_runs(opts, warmup=args.warmup, iters=args.steps, flush_l2=True)
+        # one timed run per call: L2 flushed before it, CUDA events around it
+        steps_ms = [ctx.time_runs(opts, warmup=0, iters=1, flush_l2=True) for _ in range(args.steps)]
+    ms = statistics.fmean(steps_ms)
     ranks.barrier()
     st = ctx.stats()
     launches = st.launches * args.steps
@@ -330,6 +335,7 @@ def gpu_arm(args, ranks: Ranks):
                    "y_lanes": 4, "launch": "persistent" if mode else "per-event",
                    "threads_per_event": opts.threads_per_event, "smem_bytes_per_cta": st.smem_bytes_per_cta,
                    "events_in_global_arena": st.events_in_global, "tracks": int(T.sum()),
+                   "ms_per_step_samples": [round(x, 4) for x in steps_ms],
                    "l2": "flushed between timed steps (2 x L2 memset); input also larger than L2",
                    "parallelism": f"weak scaling over {args.gpus} GPU(s), event blocks per rank"},
         "impl": "gb300",
