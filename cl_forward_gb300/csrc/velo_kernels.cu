@@ -27,6 +27,8 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "velo_internal.h"
 
 namespace velo {
@@ -615,8 +617,17 @@ int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_byte
 }
 
 int configure_search_kernel(uint32_t smem_bytes) {
-  return (int)cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem_bytes);
+  // Only ever raised, per device, so that no caller lowers it under another.
+  static std::mutex mu;
+  static uint32_t configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev >= 0 && dev < 64 && configured[dev] >= smem_bytes) return 0;
+  e = cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = smem_bytes;
+  return (int)e;
 }
 
 int search_occupancy(int block, uint32_t smem_bytes, int* ctas_per_sm) {

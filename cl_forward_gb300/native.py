@@ -44,7 +44,12 @@ EXPORTED = [
     "velo_validate_event", "velo_sort_by_x", "velo_track_capacity", "velo_search",
     "velo_search_packed", "velo_stage", "velo_run", "velo_fetch", "velo_synchronize",
     "velo_get_stats", "velo_time_runs", "velo_host_alloc", "velo_host_free", "velo_device_sm_count",
+    "velo_search_device_static",
 ]
+
+# limits of velo_search_device_static (include/velo_search.h)
+STATIC_MAX_EVENTS = 4096
+STATIC_MAX_HIT_ROWS = 131072
 
 
 class Options(ctypes.Structure):
@@ -110,6 +115,7 @@ def load() -> ctypes.CDLL:
     l.velo_host_free.argtypes = [vp, vp]
     l.velo_device_sm_count.argtypes = [vp]
     l.velo_device_sm_count.restype = i32
+    l.velo_search_device_static.argtypes = [vp, vp, vp, i32, u64, ctypes.c_uint32, i32, vp, u64, vp, vp, vp, vp]
     _lib = l
     return l
 

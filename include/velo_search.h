@@ -157,6 +157,43 @@ velo_status velo_host_free(velo_ctx* ctx, void* ptr);
 /* Number of streaming multiprocessors of the context's device. */
 int32_t velo_device_sm_count(const velo_ctx* ctx);
 
+/*
+ * Search without any device allocation.  No counterpart in the reference: it
+ * is for callers that cannot call cudaMalloc themselves -- code under a
+ * framework that owns every device allocation, or a path that must keep a
+ * fixed device footprint and may not allocate or free at run time.
+ *
+ * The caller passes device pointers: the packed events (event e at
+ * d_input + d_offsets[e], d_sizes[e] bytes, 4-byte aligned, x-sorted), and the
+ * result buffers (d_tracks_out with room for track_capacity tracks, and
+ * n_events entries of d_counts / d_first / d_status, filled as velo_search
+ * fills its host outputs).  The work is enqueued on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream) and the results are valid once it is
+ * synchronised.  Y-lanes as in velo_options; narrowing is on.
+ *
+ * All other memory is one file-scope device array of about 15 MB per GPU,
+ * held from library load to process exit.  Limits per call, rejected with
+ * VELO_ERR_CAPACITY: n_events <= VELO_STATIC_MAX_EVENTS;
+ * total_hits + n_events <= VELO_STATIC_MAX_HIT_ROWS (total_hits = the sum of
+ * the events' hit counts); track_capacity >= total_hits + n_events;
+ * max_event_hits (an upper bound on any event's hit count) small enough to
+ * stage the event in shared memory: 3,248 hits at Y = 4.  Events that break
+ * their declared bounds get VELO_EVENT_INVALID and no tracks.
+ *
+ * The first call on a device takes the array's device address (with that
+ * device current), so make that first call before any stream capture.  Every
+ * call reuses the same array: calls whose GPU work overlaps (other streams,
+ * other host threads) race and must be serialised by the caller.
+ */
+#define VELO_STATIC_MAX_EVENTS 4096
+#define VELO_STATIC_MAX_HIT_ROWS 131072
+velo_status velo_search_device_static(const uint8_t* d_input, const uint64_t* d_offsets,
+                                      const uint64_t* d_sizes, int32_t n_events, uint64_t total_hits,
+                                      uint32_t max_event_hits, int32_t y_lanes,
+                                      velo_track* d_tracks_out, uint64_t track_capacity,
+                                      uint32_t* d_counts, uint64_t* d_first, uint32_t* d_status,
+                                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif
