@@ -62,6 +62,10 @@ def parse_args():
     ap.add_argument("--threads", type=int, default=256)
     ap.add_argument("--smem-hits", type=int, default=0)
     ap.add_argument("--no-narrow", action="store_true")
+    ap.add_argument("--register-ctas", type=int, default=5, choices=[4, 5])
+    ap.add_argument("--graph", action="store_true", help="replay launches from a CUDA graph")
+    ap.add_argument("--autotune", action="store_true", help="sweep launch configurations first (cached)")
+    ap.add_argument("--e2e-chunk", type=int, default=16000, help="events per end-to-end call")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-emulator", action="store_true",
@@ -253,6 +257,9 @@ def gpu_arm(args, ranks: Ranks):
     import numpy as np
     from cl_forward_gb300 import events as E
 
+    if args.config in ("batched", "stress"):   # the batched configurations run tuned, from a graph
+        args.autotune = True
+        args.graph = True
     raw, truths = make_workload(args, ranks.rank)          # process pool before any GPU call
     blobs = sort_events(raw)
     S, H = workload_stats(blobs)
@@ -263,7 +270,8 @@ def gpu_arm(args, ranks: Ranks):
     ctx = native.Context(ranks.local)
     mode = CONFIGS[args.config][3] if args.launch is None else (1 if args.launch == "persistent" else 0)
     opts = native.default_options(threads_per_event=args.threads, launch_mode=mode,
-                                  smem_hits=args.smem_hits, narrow_windows=0 if args.no_narrow else 1)
+                                  smem_hits=args.smem_hits, narrow_windows=0 if args.no_narrow else 1,
+                                  register_ctas=args.register_ctas, use_graph=1 if args.graph else 0)
 
     # pinned host input, 16-byte aligned events
     offs = np.zeros(n, np.uint64)
@@ -279,6 +287,11 @@ def gpu_arm(args, ranks: Ranks):
     # ---- device-resident value ------------------------------------------
     ctx.stage(hbuf, offs, sizes)
     ctx.synchronize()
+    tuned = None
+    if args.autotune:
+        from cl_forward_gb300 import autotune
+        opts, tuned = autotune.tuned_options(ctx, n, float(H.mean()), opts, iters=3)
+        mode = opts.launch_mode
     ranks.barrier()
     for _ in range(args.warmup):
         ctx.run(opts)
@@ -302,23 +315,34 @@ def gpu_arm(args, ranks: Ranks):
     value = ranks.sum(n) / (ms_max / 1e3)
 
     # ---- end to end through the C ABI ------------------------------------
-    out_cap = cap
+    # chunks of at most --e2e-chunk events per call, as the reference's
+    # gpuPixelSearchByTripletInvocation chunks at 16000
+    chunk = max(1, min(args.e2e_chunk, n))
+    bounds = [(a, min(n, a + chunk)) for a in range(0, n, chunk)]
+    rows = np.maximum(H, 1).astype(np.int64)
+    out_cap = int(max(rows[a:b].sum() for a, b in bounds))
     h_tracks = ctx.host_alloc(out_cap * 100).view(E.TRACK_DTYPE)
     h_counts = np.zeros(n, np.uint32)
     h_first = np.zeros(n, np.uint64)
     h_status = np.zeros(n, np.uint32)
+
+    def e2e_pass():
+        for a, b in bounds:
+            ctx.search_packed_into(hbuf, offs[a:b], sizes[a:b], opts, h_tracks, h_counts[a:b], h_first[a:b],
+                                   h_status[a:b])
+
     for _ in range(args.warmup):
-        ctx.search_packed_into(hbuf, offs, sizes, opts, h_tracks, h_counts, h_first, h_status)
+        e2e_pass()
     ranks.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx.search_packed_into(hbuf, offs, sizes, opts, h_tracks, h_counts, h_first, h_status)
+        e2e_pass()
     e2e_s = (time.perf_counter() - t0) / args.steps
     ranks.barrier()
     e2e_max = ranks.max(e2e_s)
     assert np.array_equal(h_counts, counts)
-    h2d = int(total) + 36 * n
-    d2h = 8 + 16 * n + 100 * int(T.sum())
+    h2d = int(sum(int(offs[b - 1] + sizes[b - 1] - offs[a]) for a, b in bounds)) + 36 * n
+    d2h = 8 * len(bounds) + 16 * n + 100 * int(T.sum())
 
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
@@ -336,6 +360,9 @@ def gpu_arm(args, ranks: Ranks):
                    "threads_per_event": opts.threads_per_event, "smem_bytes_per_cta": st.smem_bytes_per_cta,
                    "events_in_global_arena": st.events_in_global, "tracks": int(T.sum()),
                    "ms_per_step_samples": [round(x, 4) for x in steps_ms],
+                   "register_ctas": opts.register_ctas, "cuda_graph": bool(opts.use_graph),
+                   "smem_hits_option": opts.smem_hits, "autotuned": tuned,
+                   "e2e_chunk_events": chunk,
                    "l2": "flushed between timed steps (2 x L2 memset); input also larger than L2",
                    "parallelism": f"weak scaling over {args.gpus} GPU(s), event blocks per rank"},
         "impl": "gb300",

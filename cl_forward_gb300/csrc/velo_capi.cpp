@@ -65,6 +65,11 @@ struct velo_ctx {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   velo_stats stats{};
   bool ran = false;
+
+  // bumped whenever buffers a captured launch refers to may have moved
+  uint64_t generation = 0;
+  cudaGraphExec_t graph = nullptr;
+  uint64_t graph_key[8] = {};
 };
 
 namespace {
@@ -180,6 +185,7 @@ void velo_default_options(velo_options* o) {
   o->narrow_windows = 1;
   o->ctas_per_sm = 0;
   o->use_graph = 0;
+  o->register_ctas = 5;
 }
 
 const char* velo_status_string(velo_status s) {
@@ -272,6 +278,7 @@ void velo_destroy(velo_ctx* c) {
                     &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
@@ -290,6 +297,7 @@ velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   c->staged = false;
   c->meta_valid = false;
   c->ran = false;
+  c->generation++;
   c->n = n;
   c->h_offset.assign(n, 0);
   c->h_hits.assign(n, 0);
@@ -332,7 +340,7 @@ velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   if ((st = ensure(c, c->d_ev_maxmod, 4ull * n, "maxmod")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_valid, 4ull * n, "valid")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_hit_base, 8ull * n, "hit_base")) != VELO_OK) return st;
-  if ((st = ensure(c, c->d_tracklets, 12ull * rows, "tracklets")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_tracklets, 16ull * rows, "tracklets")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_weak, 4ull * rows, "weak")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_tracks, sizeof(velo_track) * rows, "tracks")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_out_tracks, sizeof(velo_track) * rows, "out_tracks")) != VELO_OK) return st;
@@ -362,7 +370,20 @@ velo_status prepare_launch(velo_ctx* c, const velo_options& o, uint32_t* smem_ou
   if (o.smem_hits > 0) {
     budget = arena_layout((uint32_t)o.smem_hits, std::min<uint32_t>((uint32_t)o.smem_hits, VELO_MAX_MODULE_HITS), Y).total;
   } else {
-    budget = 68u * 1024u;   // three CTAs per SM next to the static shared state
+    // Resident CTAs per SM beat staging every event in shared memory (events
+    // over the budget run from a global-memory arena that L1 caches well), so
+    // the automatic budget stages the 40th-percentile event, within 16-100 KB.
+    std::vector<uint32_t> hits;
+    hits.reserve(c->n);
+    for (int32_t e = 0; e < c->n; ++e)
+      if (c->h_valid[e]) hits.push_back(c->h_hits[e]);
+    uint32_t hq = 0;
+    if (!hits.empty()) {
+      const size_t k = (hits.size() * 4) / 10;
+      std::nth_element(hits.begin(), hits.begin() + (std::ptrdiff_t)std::min(k, hits.size() - 1), hits.end());
+      hq = hits[std::min(k, hits.size() - 1)];
+    }
+    budget = std::max(16u * 1024u, std::min(100u * 1024u, arena_layout(hq, hq, Y).total));
   }
   const uint32_t limit = (uint32_t)std::max(0, c->max_smem_optin - 8 * 1024);
   budget = std::min(budget, limit);
@@ -403,6 +424,7 @@ velo_status prepare_launch(velo_ctx* c, const velo_options& o, uint32_t* smem_ou
                                      cudaMemcpyHostToDevice, c->stream));
     }
     c->events_in_global = nglob;
+    c->generation++;
     c->meta_valid = true;
     c->meta_smem = smem;
     c->meta_y = (int)Y;
@@ -428,16 +450,34 @@ velo_status check_options(velo_ctx* c, const velo_options* opts, velo_options* o
     return VELO_ERR_INVALID_ARGUMENT;
   }
   o->threads_per_event = (int32_t)resolve_threads(o->threads_per_event);
+  if (o->register_ctas == 0) o->register_ctas = 5;
+  if (o->register_ctas != 4 && o->register_ctas != 5) {
+    c->err = "register_ctas must be 4 or 5";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
+  return VELO_OK;
+}
+
+// Grid of the launch (the occupancy query stays outside any stream capture).
+velo_status launch_shape(velo_ctx* c, const velo_options& o, uint32_t smem, int* grid) {
+  *grid = c->n;
+  if (o.launch_mode == VELO_LAUNCH_PERSISTENT && c->n > 0) {
+    int per_sm = o.ctas_per_sm;
+    if (per_sm <= 0) {
+      int occ = 0;
+      int e = velo::search_occupancy(o.threads_per_event, smem, o.register_ctas, &occ);
+      if (e != 0) return cuda_fail(c, (cudaError_t)e, "occupancy");
+      per_sm = std::max(occ, 1);
+    }
+    *grid = (int)std::min<int64_t>((int64_t)c->sm_count * per_sm, c->n);
+  }
   return VELO_OK;
 }
 
 // memset of the queue head / output cursor, then the search kernel.
-velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
+velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, int grid) {
   VELO_CUDA(c, cudaMemsetAsync(c->d_counters.p, 0, 64, c->stream));
-  if (c->n == 0) {
-    c->stats.launches = 0;
-    return VELO_OK;
-  }
+  if (c->n == 0) return VELO_OK;
   velo::SearchParams p{};
   p.input = P<uint8_t>(c->d_input);
   p.ev_offset = P<uint64_t>(c->d_ev_offset);
@@ -462,24 +502,46 @@ velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
   p.out_status = P<uint32_t>(c->d_out_status);
   p.out_cursor = P<unsigned long long>(c->d_counters);
   p.work_counter = reinterpret_cast<int32_t*>(P<uint8_t>(c->d_counters) + 32);
-  const int block = o.threads_per_event;
-  int grid = c->n;
-  if (p.persistent) {
-    int per_sm = o.ctas_per_sm;
-    if (per_sm <= 0) {
-      int occ = 0;
-      int e = velo::search_occupancy(block, smem, &occ);
-      if (e != 0) return cuda_fail(c, (cudaError_t)e, "occupancy");
-      per_sm = std::max(occ, 1);
-    }
-    grid = std::min<int64_t>((int64_t)c->sm_count * per_sm, c->n);
-  }
-  int e = velo::launch_search(p, grid, block, smem, c->stream);
+  int e = velo::launch_search(p, grid, o.threads_per_event, smem, c->stream, o.register_ctas);
   if (e != 0) return cuda_fail(c, (cudaError_t)e, "search kernel launch");
-  c->stats.launches = 1;
+  return VELO_OK;
+}
+
+// One run: directly, or by replaying a CUDA graph of the same two operations
+// (captured once per staged batch and launch configuration).
+velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
+  int grid = 0;
+  velo_status st = launch_shape(c, o, smem, &grid);
+  if (st != VELO_OK) return st;
+  c->stats.launches = c->n > 0 ? 1u : 0u;
   c->stats.grid = grid;
-  c->stats.block = block;
+  c->stats.block = o.threads_per_event;
   c->stats.smem_bytes_per_cta = (int32_t)smem;
+  if (!o.use_graph) return enqueue_kernel(c, o, smem, grid);
+  const uint64_t key[8] = {c->generation, smem, (uint64_t)grid, (uint64_t)o.threads_per_event,
+                           (uint64_t)o.register_ctas, (uint64_t)o.y_lanes, (uint64_t)o.narrow_windows,
+                           (uint64_t)o.launch_mode};
+  if (!c->graph || std::memcmp(key, c->graph_key, sizeof key) != 0) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    VELO_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    st = enqueue_kernel(c, o, smem, grid);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (st != VELO_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ce != cudaSuccess) return cuda_fail(c, ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      c->graph = nullptr;
+      return cuda_fail(c, ce, "cudaGraphInstantiate");
+    }
+    std::memcpy(c->graph_key, key, sizeof key);
+  }
+  VELO_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
   return VELO_OK;
 }
 
@@ -642,6 +704,47 @@ velo_status velo_time_runs(velo_ctx* c, const velo_options* opts, int32_t warmup
   c->stats.total_hits = c->total_hits;
   c->stats.input_bytes = c->input_bytes;
   c->stats.events_in_global = c->events_in_global;
+  return VELO_OK;
+}
+
+velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, velo_options* best_out,
+                          float* best_ms_out) {
+  if (!c || !best_out || iters <= 0) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->staged) return VELO_ERR_NOT_STAGED;
+  velo_options b0;
+  velo_status st = check_options(c, base, &b0);
+  if (st != VELO_OK) return st;
+  // threads per event x shared-memory tile (hits staged per CTA; 0 = the
+  // automatic budget) x register build x launch style; narrowing stays on
+  // (it only removes work) and y_lanes is the caller's (it defines results)
+  static const int32_t kThreads[] = {128, 256};
+  static const int32_t kSmemHits[] = {0, 600, 900, 1200, 1600, 2400};
+  static const int32_t kRegs[] = {4, 5};
+  static const int32_t kModes[] = {VELO_LAUNCH_PER_EVENT, VELO_LAUNCH_PERSISTENT};
+  float best = 0.f;
+  bool have = false;
+  for (int32_t mode : kModes)
+    for (int32_t regs : kRegs)
+      for (int32_t threads : kThreads)
+        for (int32_t hits : kSmemHits) {
+          velo_options o = b0;
+          o.launch_mode = mode;
+          o.register_ctas = regs;
+          o.threads_per_event = threads;
+          o.smem_hits = hits;
+          o.narrow_windows = 1;
+          std::vector<float> ms(iters);
+          for (int32_t i = 0; i < iters; ++i)
+            if ((st = velo_time_runs(c, &o, i == 0 ? 1 : 0, 1, 1, &ms[i])) != VELO_OK) return st;
+          std::nth_element(ms.begin(), ms.begin() + iters / 2, ms.end());
+          const float med = ms[iters / 2];
+          if (!have || med < best) {
+            best = med;
+            *best_out = o;
+            have = true;
+          }
+        }
+  if (best_ms_out) *best_ms_out = best;
   return VELO_OK;
 }
 

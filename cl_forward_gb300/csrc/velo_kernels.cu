@@ -23,6 +23,15 @@
 // range bounds it; a 0.01 mm guard covers the rounding of the bound).  On an
 // unsorted module the full sequential scan runs.  Narrowing changes work, not
 // results.
+//
+// Per module iteration the CTA meets at two barriers: after forwarding (its
+// used-hit marks feed seeding) and after seeding (its tracklets feed the next
+// forwarding).  Seeding gives each h0 to one warp, whose lanes take the h0's
+// h1 candidates; lane cut-offs come from a ballot and the winner from a warp
+// min-reduction, so seeding itself needs no block barrier.  Each
+// tracks-to-follow buffer is filled from both ends (forwarding from the
+// front, seeding from the back), which keeps the two counts separate without
+// another barrier.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
@@ -38,6 +47,9 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint32_t kNone16 = 0xffffu;
+
 struct Shared {
   int32_t start[kMaxModules + 1];
   int32_t num[kMaxModules + 1];
@@ -45,24 +57,23 @@ struct Shared {
   float zmin[kMaxModules + 1];
   float zmax[kMaxModules + 1];
   uint8_t sorted[kMaxModules + 1];
-  uint32_t ncur, nnext, ntracks, ntracklets, nweak, status, nslots, ntasks;
+  uint32_t ring_lo[2];   // forwarding entries, from the front of ring[i]
+  uint32_t ring_hi[2];   // seeding entries, from the back of ring[i]
+  uint32_t ntracks, ntracklets, nweak, status;
   unsigned long long out_first;
   int32_t next_event;
 };
 
 struct EventView {
   int S, H, Y;
-  uint32_t cap;             // capacity of tracklet / track / weak rows (max(H, 1))
+  uint32_t cap;             // tracklet / track / weak rows (max(H, 1))
   uint32_t ring_cap;        // entries of each tracks-to-follow buffer (H + 1)
   float *x, *y, *z;
-  int32_t *h1f, *h1l, *h2f, *h2l;
+  uint2* win;               // per hit: {h1 first | h1 last << 16, h2 first | h2 last << 16}
   uint8_t* used;
-  uint32_t *ring0, *ring1;
-  int32_t* slot_h0;
-  uint32_t* slot_pref;
-  uint32_t* cutoff;
-  unsigned long long* best;
-  uint32_t* tracklets;
+  uint32_t* ring0;          // tracks-to-follow buffers, selected by parity
+  uint32_t* ring1;
+  uint4* tracklets;         // {h0, h1, h2, 0} per tracklet
   uint32_t* weak;
   velo_track* tracks;
   bool narrow;
@@ -77,24 +88,31 @@ __device__ __forceinline__ int first_gt(const float* x, int lo, int hi, float c)
   return lo;
 }
 
-// Index range [lo, hi) of a sorted module outside which no hit can satisfy
-// |fl(xp - x)| < tol for any predicted xp in [xl, xh].
-__device__ __forceinline__ void narrow_range(const float* x, int n, float xl, float xh, float tol,
+// Sub-range [lo, hi) of [lo0, hi0) on a sorted module outside which no hit
+// can satisfy |fl(xp - x)| < tol for any predicted xp in [xl, xh].  The upper
+// end is usually a few hits past the lower one: walk, then bisect.
+__device__ __forceinline__ void narrow_range(const float* x, int lo0, int hi0, float xl, float xh, float tol,
                                              int* lo, int* hi) {
   const float margin = fadd(0.01f, fmul(1e-5f, fadd(fabsf(xl), fabsf(xh))));
   const float lt = fsub(fsub(xl, tol), margin);
   const float ht = fadd(fadd(xh, tol), margin);
   if (isfinite(lt) && isfinite(ht)) {
-    *lo = first_gt(x, 0, n, lt);
-    *hi = first_gt(x, *lo, n, ht);
+    const int l = first_gt(x, lo0, hi0, lt);
+    int h = l;
+    const int walk_end = min(hi0, l + 8);
+    while (h < walk_end && !(x[h] > ht)) ++h;
+    if (h == walk_end && h < hi0) h = first_gt(x, h, hi0, ht);
+    *lo = l;
+    *hi = h;
   } else {
-    *lo = 0;
-    *hi = n;
+    *lo = lo0;
+    *hi = hi0;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Candidate windows of hit h on module f (Kernel.cl:50-178).
+// Candidate windows of hit h on module f (Kernel.cl:50-178), stored relative
+// to the start of module f-2 (0xffff = none).
 __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int f) {
   const int s2 = f - 2;
   const bool proc_h2 = f <= ev.S - 3;
@@ -103,7 +121,7 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
   const float* x2 = ev.x + st2;
   const float* z2 = ev.z + st2;
   const bool sorted = ev.narrow && s.sorted[s2];
-  int r1f = -1, r1l = -1, r2f = -1, r2l = -1;
+  uint32_t r1f = kNone16, r1l = kNone16, r2f = kNone16, r2l = kNone16;
 
   // h1 window: first hit with |x1-x0| < 0.7|z1-z0|, then the first later hit
   // that fails it (Kernel.cl:115-135,161-165).
@@ -113,7 +131,7 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
       const float da = fabsf(fsub(s.zmin[s2], z0));
       const float db = fabsf(fsub(s.zmax[s2], z0));
       const float D = fmul(kMaxXSlopeCandidates, fmaxf(da, db));   // >= every hit's dxmax
-      narrow_range(x2, n2, x0, x0, D, &lo, &hi);
+      narrow_range(x2, 0, n2, x0, x0, D, &lo, &hi);
     }
     bool found = false;
     for (int e = lo; e < hi; ++e) {
@@ -121,13 +139,13 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
       const float dxmax = fmul(kMaxXSlopeCandidates, h_dist);
       const bool tol = fabsf(fsub(x2[e], x0)) < dxmax;
       if (!found) {
-        if (tol) { found = true; r1f = st2 + e; }
+        if (tol) { found = true; r1f = (uint32_t)e; }
       } else if (!tol) {
-        r1l = st2 + e;
+        r1l = (uint32_t)e;
         break;
       }
     }
-    if (found && r1l < 0) r1l = st2 + hi;   // hit `hi` provably fails, or hi is the end
+    if (found && r1l == kNone16) r1l = (uint32_t)hi;   // hit `hi` provably fails, or hi is the end
   }
 
   // h2 window for h taken as the h1 of a seed on f+2 (Kernel.cl:85-102,137-150).
@@ -144,275 +162,320 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
     if (sorted) {   // `x > c` is monotone on a non-decreasing module: exact
       const int a = first_gt(x2, 0, n2, xmin_h2);
       if (a < n2) {
-        r2f = st2 + a;
-        r2l = st2 + first_gt(x2, a + 1, n2, xmax_h2);
+        r2f = (uint32_t)a;
+        r2l = (uint32_t)first_gt(x2, a + 1, n2, xmax_h2);
       }
     } else {
       bool found = false;
       for (int e = 0; e < n2; ++e) {
         if (!found) {
-          if (x2[e] > xmin_h2) { found = true; r2f = st2 + e; }
+          if (x2[e] > xmin_h2) { found = true; r2f = (uint32_t)e; }
         } else if (x2[e] > xmax_h2) {
-          r2l = st2 + e;
+          r2l = (uint32_t)e;
           break;
         }
       }
-      if (found && r2l < 0) r2l = st2 + n2;
+      if (found && r2l == kNone16) r2l = (uint32_t)n2;
     }
   }
-  ev.h1f[h] = r1f;
-  ev.h1l[h] = r1l;
-  ev.h2f[h] = r2f;
-  ev.h2l[h] = r2l;
+  ev.win[h] = make_uint2(r1f | (r1l << 16), r2f | (r2l << 16));
 }
 
 // ---------------------------------------------------------------------------
-// fitHitToTrack (Kernel.cl:15-35): the scatter, FLT_MAX when a cut fails, or
-// NaN where the reference's `condition*scatter + !condition*MAX` is NaN.
-__device__ __forceinline__ float fit_hit(float tx, float ty, float h0x, float h0y, float h0z,
-                                         float h1z, float h2x, float h2y, float h2z) {
-  const float dz = fsub(h2z, h0z);
-  const float dx = fabsf(fsub(fadd(h0x, fmul(tx, dz)), h2x));
-  const float dy = fabsf(fsub(fadd(h0y, fmul(ty, dz)), h2y));
-  const float num = fadd(fmul(dx, dx), fmul(dy, dy));
-  const float den = fdiv(1.f, fsub(h2z, h1z));
-  const float scatter = fmul(fmul(num, den), den);
-  if (dx < kTolerance && dy < kTolerance && scatter < kMaxScatter) return scatter;
-  return isfinite(scatter) ? FLT_MAX : __int_as_float(0x7fc00000);
+// Tracks-to-follow entries.  Bit 31 marks a tracklet (3 hits, number = its
+// row in the tracklet list) and bits 28-30 count skipped modules, as in the
+// reference (Kernel.cl:222-225,351,566).  This build also keeps a track's
+// hit count in bits 23-27 (the reference re-reads it from the track), so
+// numbers use bits 0-22.
+constexpr uint32_t kEntryNumber = 0x007FFFFFu;
+constexpr uint32_t kEntryCountShift = 23;
+
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+// One shared-memory atomic per warp: lanes with `take` get consecutive slots
+// from *counter; returns this lane's slot.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, bool take) {
+  const unsigned m = __ballot_sync(kFull, take);
+  if (m == 0) return 0;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  return base + (uint32_t)__popc(m & lanemask_lt());
 }
 
-__device__ __forceinline__ void push_ring(Shared& s, const EventView& ev, uint32_t* nxt, uint32_t v) {
-  const uint32_t i = atomicAdd(&s.nnext, 1u);
-  if (i < ev.ring_cap) nxt[i] = v;
+// (a select, not an indexed array, so the view stays in registers)
+__device__ __forceinline__ uint32_t* ring_buf(const EventView& ev, int b) { return b ? ev.ring1 : ev.ring0; }
+
+__device__ __forceinline__ void push_back(Shared& s, const EventView& ev, int b, uint32_t v) {
+  const uint32_t i = atomicAdd(&s.ring_hi[b], 1u);
+  if (i < ev.ring_cap) ring_buf(ev, b)[ev.ring_cap - 1u - i] = v;
 }
 
-// Track forwarding of one tracks-to-follow entry onto module m4
-// (Kernel.cl:210-367).
-__device__ void forward_entry(const EventView& ev, Shared& s, uint32_t full, int m4, uint32_t* nxt) {
-  const bool is_tracklet = (full & kTrackletFlag) != 0;
-  const uint32_t skipped = (full & kSkipMask) >> 28;
-  uint32_t trackno = full & kNumberMask;
-  uint32_t n, h0, h1, t0 = 0, t1 = 0, t2 = 0;
-  if (is_tracklet) {
-    t0 = ev.tracklets[3 * trackno + 0];
-    t1 = ev.tracklets[3 * trackno + 1];
-    t2 = ev.tracklets[3 * trackno + 2];
-    n = 3;
-    h0 = t1;
-    h1 = t2;
-  } else {
-    const velo_track& t = ev.tracks[trackno];
-    n = t.hitsNum;
-    h0 = t.hits[n - 2];
-    h1 = t.hits[n - 1];
-  }
-  const float h0x = ev.x[h0], h0y = ev.y[h0], h0z = ev.z[h0];
-  const float h1x = ev.x[h1], h1y = ev.y[h1], h1z = ev.z[h1];
-  const float td = fdiv(1.0f, fsub(h1z, h0z));
-  const float tx = fmul(fsub(h1x, h0x), td);
-  const float ty = fmul(fsub(h1y, h0y), td);
+// i-th entry of ring[b]: the front segment, then the back segment.
+__device__ __forceinline__ uint32_t ring_entry(const EventView& ev, int b, uint32_t lo, uint32_t i) {
+  const uint32_t* r = ring_buf(ev, b);
+  return i < lo ? r[i] : r[ev.ring_cap - 1u - (i - lo)];
+}
 
-  const int st4 = s.start[m4], n4 = s.num[m4];
-  const float* x4 = ev.x + st4;
-  int lo = 0, hi = n4;
-  if (ev.narrow && s.sorted[m4] && n4 > 0) {
-    const float xa = fadd(h0x, fmul(tx, fsub(s.zmin[m4], h0z)));
-    const float xb = fadd(h0x, fmul(tx, fsub(s.zmax[m4], h0z)));
-    if (isfinite(xa) && isfinite(xb)) narrow_range(x4, n4, fminf(xa, xb), fmaxf(xa, xb), kTolerance, &lo, &hi);
-  }
-  float best = FLT_MAX;
-  int best_h2 = -1;
-  bool degenerate = false;
-  for (int k = lo; k < hi; ++k) {
-    const int h2 = st4 + k;
-    const float fit = fit_hit(tx, ty, h0x, h0y, h0z, h1z, x4[k], ev.y[h2], ev.z[h2]);
-    if (isnan(fit)) { degenerate = true; continue; }
-    if (fit < best) { best = fit; best_h2 = h2; }
-  }
-  if (degenerate) atomicOr(&s.status, VELO_EVENT_DEGENERATE);
-
-  if (best != FLT_MAX) {
-    if (n >= VELO_MAX_TRACK_SIZE) {   // the reference writes past hits[24] here
-      atomicOr(&s.status, VELO_EVENT_TRACK_OVERFLOW);
-      return;
-    }
-    ev.used[best_h2] = 1;
-    if (is_tracklet) {   // third -> fourth hit: allocate a track, mark hits 0-2
-      ev.used[t0] = 1;
-      ev.used[t1] = 1;
-      ev.used[t2] = 1;
-      const uint32_t tn = atomicAdd(&s.ntracks, 1u);
-      if (tn >= ev.cap) return;
-      uint32_t* w = reinterpret_cast<uint32_t*>(&ev.tracks[tn]);
-      w[0] = 4; w[1] = t0; w[2] = t1; w[3] = t2; w[4] = (uint32_t)best_h2;
-#pragma unroll
-      for (int i = 5; i < 25; ++i) w[i] = 0;
-      trackno = tn;
+// Track forwarding onto module m4 (Kernel.cl:210-367), one warp at a time:
+// lane j forwards entry i0 + j of ring[b].  Track numbers, ring slots and
+// weak slots are reserved with one atomic per warp; new entries go to the
+// front of ring[nb].
+__device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_n, uint32_t i0, uint32_t ncur,
+                             int m4, int nb) {
+  enum { kNone = 0, kPushTrack, kNewTrack, kPushSkip, kWeak };
+  const uint32_t i = i0 + (threadIdx.x & 31);
+  int action = kNone;
+  uint32_t push_value = 0, trackno = 0, best_h2 = 0;
+  uint4 tl = make_uint4(0, 0, 0, 0);
+  if (i < ncur) {
+    const uint32_t full = ring_entry(ev, b, lo_n, i);
+    const bool is_tracklet = (full & kTrackletFlag) != 0;
+    const uint32_t skipped = (full & kSkipMask) >> 28;
+    trackno = full & kEntryNumber;
+    uint32_t n, h0, h1;
+    if (is_tracklet) {
+      tl = ev.tracklets[trackno];
+      n = 3;
+      h0 = tl.y;
+      h1 = tl.z;
     } else {
-      velo_track& t = ev.tracks[trackno];
-      t.hits[n] = (uint32_t)best_h2;
-      t.hitsNum = n + 1;
+      n = (full >> kEntryCountShift) & 31u;
+      const velo_track& t = ev.tracks[trackno];
+      h0 = t.hits[n - 2];
+      h1 = t.hits[n - 1];
     }
-    push_ring(s, ev, nxt, trackno);
-  } else if (skipped <= kMaxSkippedModules) {
-    push_ring(s, ev, nxt, ((skipped + 1u) << 28) | (full & 0x8FFFFFFFu));
-  } else if (is_tracklet) {
-    const uint32_t wi = atomicAdd(&s.nweak, 1u);
-    if (wi < ev.cap) ev.weak[wi] = trackno;
-  }
-}
+    const float h0x = ev.x[h0], h0y = ev.y[h0], h0z = ev.z[h0];
+    const float h1x = ev.x[h1], h1y = ev.y[h1], h1z = ev.z[h1];
+    const float td = fdiv(1.0f, fsub(h1z, h0z));
+    const float tx = fmul(fsub(h1x, h0x), td);
+    const float ty = fmul(fsub(h1y, h0y), td);
 
-// Last slot whose prefix is <= t (prefixes strictly increase).
-__device__ __forceinline__ int slot_of(const uint32_t* pref, int nslots, uint32_t t) {
-  int lo = 0, hi = nslots - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (pref[mid] <= t) lo = mid; else hi = mid - 1;
+    const int st4 = s.start[m4], n4 = s.num[m4];
+    const float* x4 = ev.x + st4;
+    const float* y4 = ev.y + st4;
+    const float* z4 = ev.z + st4;
+    int lo = 0, hi = n4;
+    if (ev.narrow && s.sorted[m4] && n4 > 0) {
+      const float xa = fadd(h0x, fmul(tx, fsub(s.zmin[m4], h0z)));
+      const float xb = fadd(h0x, fmul(tx, fsub(s.zmax[m4], h0z)));
+      if (isfinite(xa) && isfinite(xb)) narrow_range(x4, 0, n4, fminf(xa, xb), fmaxf(xa, xb), kTolerance, &lo, &hi);
+    }
+    // fitHitToTrack (Kernel.cl:15-35) over the candidates, first minimum wins.
+    // The scatter's 1/(z2 - z1) depends only on z2 here: it is recomputed only
+    // when z2's bit pattern changes (same operands, same rounded value).
+    float best = FLT_MAX;
+    int best_k = -1;
+    bool degenerate = false;
+    uint32_t zc = 0x7fc00001u;   // bit pattern of the z2 the cached factor belongs to (none yet)
+    float den = 0.f;
+    for (int k = lo; k < hi; ++k) {
+      const float h2z = z4[k];
+      if (__float_as_uint(h2z) != zc) {
+        zc = __float_as_uint(h2z);
+        den = fdiv(1.f, fsub(h2z, h1z));
+      }
+      const float dz = fsub(h2z, h0z);
+      const float dx = fabsf(fsub(fadd(h0x, fmul(tx, dz)), x4[k]));
+      const float dy = fabsf(fsub(fadd(h0y, fmul(ty, dz)), y4[k]));
+      const float scatter = fmul(fmul(fadd(fmul(dx, dx), fmul(dy, dy)), den), den);
+      if (dx < kTolerance && dy < kTolerance && scatter < kMaxScatter) {
+        if (scatter < best) { best = scatter; best_k = k; }
+      } else if (!isfinite(scatter)) {
+        degenerate = true;   // the reference's `condition*scatter + !condition*MAX` is NaN here
+      }
+    }
+    if (degenerate) atomicOr(&s.status, VELO_EVENT_DEGENERATE);
+
+    if (best_k >= 0) {
+      best_h2 = (uint32_t)(st4 + best_k);
+      if (n >= VELO_MAX_TRACK_SIZE) {   // the reference writes past hits[24] here
+        atomicOr(&s.status, VELO_EVENT_TRACK_OVERFLOW);
+      } else {
+        ev.used[best_h2] = 1;
+        if (is_tracklet) {   // third -> fourth hit: a track is allocated below; hits 0-2 marked
+          ev.used[tl.x] = 1;
+          ev.used[tl.y] = 1;
+          ev.used[tl.z] = 1;
+          action = kNewTrack;
+        } else {
+          velo_track& t = ev.tracks[trackno];
+          t.hits[n] = best_h2;
+          t.hitsNum = n + 1;
+          action = kPushTrack;
+          push_value = trackno | ((n + 1u) << kEntryCountShift);
+        }
+      }
+    } else if (skipped <= kMaxSkippedModules) {
+      action = kPushSkip;
+      push_value = ((skipped + 1u) << 28) | (full & 0x8FFFFFFFu);
+    } else if (is_tracklet) {
+      action = kWeak;
+    }
   }
-  return lo;
+  // new tracks (Kernel.cl:324-337)
+  const uint32_t tn = warp_reserve(&s.ntracks, action == kNewTrack);
+  if (action == kNewTrack) {
+    if (tn < ev.cap) {
+      uint32_t* w = reinterpret_cast<uint32_t*>(&ev.tracks[tn]);
+      w[0] = 4; w[1] = tl.x; w[2] = tl.y; w[3] = tl.z; w[4] = best_h2;
+#pragma unroll
+      for (int k = 5; k < 25; ++k) w[k] = 0;
+      push_value = tn | (4u << kEntryCountShift);
+    } else {
+      action = kNone;
+    }
+  }
+  // tracks to follow in the next iteration (Kernel.cl:344-355)
+  const bool push = action == kPushTrack || action == kNewTrack || action == kPushSkip;
+  const uint32_t slot = warp_reserve(&s.ring_lo[nb], push);
+  if (push && slot < ev.ring_cap) ring_buf(ev, nb)[slot] = push_value;
+  // three-hit tracklets that ran out of skips (Kernel.cl:359-363)
+  const uint32_t wi = warp_reserve(&s.nweak, action == kWeak);
+  if (action == kWeak && wi < ev.cap) ev.weak[wi] = trackno;
 }
 
 // Seeding of module f: h0 on f, h1 on f-2, h2 on f-4 (Kernel.cl:392-568
-// with the unused-h0 gather of :720-764).  Work is flattened over (h0, h1
-// element) pairs; each pair scans its h2 window and folds its first minimum
-// into the h0's packed key with a shared-memory atomicMin.
-__device__ void seed_module(const EventView& ev, Shared& s, int f, uint32_t* nxt) {
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+// with the unused-h0 gather of :720-764).  One warp per h0; lane j of chunk c
+// takes h1 element e = 32c + j, which belongs to the reference's Y-lane
+// e mod Y.  New tracklets go to the back of ring[nb].
+__device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint32_t below_same_lane,
+                            uint32_t lane_mod) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int st0 = s.start[f], n0 = s.num[f];
-  const int Y = ev.Y;
-
-  // S1: unused h0 with a non-empty h1 window, and the prefix of window sizes
-  if (tid < 32) {
-    uint32_t nslots = 0, ntasks = 0;
-    for (int c = 0; c < n0; c += 32) {
-      const int i = c + lane;
-      const int h0 = st0 + i;
-      uint32_t n1 = 0;
-      if (i < n0 && !ev.used[h0]) {
-        const int a = ev.h1f[h0];
-        n1 = a >= 0 ? (uint32_t)(ev.h1l[h0] - a) : 0u;
-      }
-      const unsigned take = __ballot_sync(0xffffffffu, n1 > 0);
-      uint32_t inc = n1;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += v;
-      }
-      if (n1 > 0) {
-        const uint32_t pos = nslots + __popc(take & ((1u << lane) - 1u));
-        ev.slot_h0[pos] = h0;
-        ev.slot_pref[pos] = ntasks + inc - n1;
-      }
-      nslots += __popc(take);
-      ntasks += __shfl_sync(0xffffffffu, inc, 31);
-    }
-    if (lane == 0) {
-      s.nslots = nslots;
-      s.ntasks = ntasks;
-      ev.slot_pref[nslots] = ntasks;
-    }
-  }
-  __syncthreads();
-  const int nslots = (int)s.nslots;
-  const uint32_t ntasks = s.ntasks;
-  if (nslots == 0) return;   // uniform
-
-  // S2: reset per-slot state
-  for (int i = tid; i < nslots * Y; i += nt) ev.cutoff[i] = 0xffffffffu;
-  for (int i = tid; i < nslots; i += nt) ev.best[i] = ~0ull;
-  __syncthreads();
-
-  // S3: each lane's first h1 element without an h2 window
-  for (uint32_t t = tid; t < ntasks; t += nt) {
-    const int sl = slot_of(ev.slot_pref, nslots, t);
-    const uint32_t e = t - ev.slot_pref[sl];
-    const int h1 = ev.h1f[ev.slot_h0[sl]] + (int)e;
-    if (ev.h2f[h1] == -1) atomicMin(&ev.cutoff[sl * Y + (int)(e % (uint32_t)Y)], e);
-  }
-  __syncthreads();
-
-  // S4: triplet scatter search
   const int s1 = f - 2, m4 = f - 4;
-  const int st4 = s.start[m4], n4 = s.num[m4];
-  const float s1_z = s.num[s1] > 0 ? ev.z[s.start[s1]] : 0.f;   // Kernel.cl:420
+  const int st1 = s.start[s1], st4 = s.start[m4], n4 = s.num[m4];
+  const uint32_t Y = (uint32_t)ev.Y;
+  const uint32_t chunk_step = 32u % Y;
+  const float s1_z = s.num[s1] > 0 ? ev.z[st1] : 0.f;   // Kernel.cl:420
   const bool narrow4 = ev.narrow && s.sorted[m4] && n4 > 0;
   const float zmin4 = s.zmin[m4], zmax4 = s.zmax[m4];
+  const float* x4 = ev.x + st4;
+  const float* y4 = ev.y + st4;
+  const float* z4 = ev.z + st4;
   bool degenerate = false;
-  for (uint32_t t = tid; t < ntasks; t += nt) {
-    const int sl = slot_of(ev.slot_pref, nslots, t);
-    const uint32_t e = t - ev.slot_pref[sl];
-    const uint32_t lane_y = e % (uint32_t)Y;
-    if (e >= ev.cutoff[sl * Y + (int)lane_y]) continue;
-    const int h0 = ev.slot_h0[sl];
-    const int h1 = ev.h1f[h0] + (int)e;
-    if (ev.used[h1]) continue;
+
+  for (int i = warp; i < n0; i += nwarps) {
+    const int h0 = st0 + i;
+    if (ev.used[h0]) continue;                       // warp-uniform
+    const uint32_t w0 = ev.win[h0].x;
+    const uint32_t f1 = w0 & 0xffffu;
+    if (f1 == kNone16) continue;
+    const int n1 = (int)(w0 >> 16) - (int)f1;        // > 0 when a first hit was found
     const float h0x = ev.x[h0], h0y = ev.y[h0], h0z = ev.z[h0];
-    const float h1x = ev.x[h1], h1y = ev.y[h1], h1z = ev.z[h1];
     const float dymax = fmul(kMaxYSlope, fabsf(fsub(s1_z, h0z)));
-    if (!(fabsf(fsub(h1y, h0y)) < dymax)) continue;   // h2-independent term of Kernel.cl:509
-    const float dz_inverted = fdiv(1.f, fsub(h1z, h0z));
-    const float ddx = fsub(h1x, h0x), ddy = fsub(h1y, h0y);
-    int a = ev.h2f[h1], b = ev.h2l[h1];
-    if (narrow4) {
-      const float xa = fadd(h0x, fmul(ddx, fmul(fsub(zmin4, h0z), dz_inverted)));
-      const float xb = fadd(h0x, fmul(ddx, fmul(fsub(zmax4, h0z), dz_inverted)));
-      if (isfinite(xa) && isfinite(xb)) {
-        int lo, hi;
-        narrow_range(ev.x + st4, n4, fminf(xa, xb), fmaxf(xa, xb), kTolerance, &lo, &hi);
-        a = max(a, st4 + lo);
-        b = min(b, st4 + hi);
-      }
-    }
-    float lbest = FLT_MAX;
-    int lh2 = -1;
-    for (int h2 = a; h2 < b; ++h2) {
-      const float h2x = ev.x[h2], h2y = ev.y[h2], h2z = ev.z[h2];
-      const float z2_tz = fmul(fsub(h2z, h0z), dz_inverted);
-      const float dx = fsub(fadd(h0x, fmul(ddx, z2_tz)), h2x);
-      const float dy = fsub(fadd(h0y, fmul(ddy, z2_tz)), h2y);
-      if (fabsf(dx) < kTolerance && fabsf(dy) < kTolerance) {
-        const float num = fadd(fmul(dx, dx), fmul(dy, dy));
-        const float den = fdiv(1.f, fsub(h2z, h1z));
-        const float scatter = fmul(fmul(num, den), den);
-        if (scatter < kMaxScatter) {
-          if (scatter < lbest) { lbest = scatter; lh2 = h2; }
-        } else if (!isfinite(scatter)) {
-          degenerate = true;
+    unsigned long long best = ~0ull;
+    uint32_t dead_lanes = 0;                         // Y-lanes already stopped (bit per lane)
+    uint32_t chunk_mod = 0;
+    for (int c = 0; c < n1; c += 32) {
+      const int e = c + lane;
+      const bool in = e < n1;
+      uint32_t ly = lane_mod + chunk_mod;
+      if (ly >= Y) ly -= Y;
+      const int h1 = st1 + (int)f1 + e;
+      uint32_t w1 = 0;
+      if (in) w1 = ev.win[h1].y;
+      const bool dead = in && (w1 & 0xffffu) == kNone16;
+      const unsigned dmask = __ballot_sync(kFull, dead);
+      const bool stopped = ((dmask & below_same_lane) != 0) || ((dead_lanes >> ly) & 1u);
+      dead_lanes |= __reduce_or_sync(kFull, dead ? (1u << ly) : 0u);
+      chunk_mod += chunk_step;
+      if (chunk_mod >= Y) chunk_mod -= Y;
+      if (!in || dead || stopped || ev.used[h1]) continue;
+      const float h1x = ev.x[h1], h1y = ev.y[h1], h1z = ev.z[h1];
+      if (!(fabsf(fsub(h1y, h0y)) < dymax)) continue;   // h2-independent term of Kernel.cl:509
+      const float dz_inverted = fdiv(1.f, fsub(h1z, h0z));
+      const float ddx = fsub(h1x, h0x), ddy = fsub(h1y, h0y);
+      int a = (int)(w1 & 0xffffu), b = (int)(w1 >> 16);
+      if (narrow4) {
+        const float xa = fadd(h0x, fmul(ddx, fmul(fsub(zmin4, h0z), dz_inverted)));
+        const float xb = fadd(h0x, fmul(ddx, fmul(fsub(zmax4, h0z), dz_inverted)));
+        if (isfinite(xa) && isfinite(xb) && a < b) {
+          int lo, hi;
+          narrow_range(x4, a, b, fminf(xa, xb), fmaxf(xa, xb), kTolerance, &lo, &hi);
+          a = lo;
+          b = hi;
         }
       }
+      float lbest = FLT_MAX;
+      int lk = -1;
+      uint32_t zc = 0x7fc00001u;
+      float z2_tz = 0.f, den = 0.f;
+      for (int k = a; k < b; ++k) {
+        const float h2z = z4[k];
+        if (__float_as_uint(h2z) != zc) {   // both factors depend on h2z only (per h0, h1)
+          zc = __float_as_uint(h2z);
+          z2_tz = fmul(fsub(h2z, h0z), dz_inverted);
+          den = fdiv(1.f, fsub(h2z, h1z));
+        }
+        const float dx = fsub(fadd(h0x, fmul(ddx, z2_tz)), x4[k]);
+        const float dy = fsub(fadd(h0y, fmul(ddy, z2_tz)), y4[k]);
+        if (fabsf(dx) < kTolerance && fabsf(dy) < kTolerance) {
+          const float scatter = fmul(fmul(fadd(fmul(dx, dx), fmul(dy, dy)), den), den);
+          if (scatter < kMaxScatter) {
+            if (scatter < lbest) { lbest = scatter; lk = k; }
+          } else if (!isfinite(scatter)) {
+            degenerate = true;
+          }
+        }
+      }
+      if (lk >= 0) {
+        const unsigned long long key = ((unsigned long long)__float_as_uint(lbest) << 32) |
+                                       ((unsigned long long)ly << 28) | ((unsigned long long)e << 14) |
+                                       (unsigned long long)lk;
+        best = key < best ? key : best;
+      }
     }
-    if (lh2 >= 0) {
-      const unsigned long long key = ((unsigned long long)__float_as_uint(lbest) << 32) |
-                                     ((unsigned long long)lane_y << 28) |
-                                     ((unsigned long long)e << 14) | (unsigned long long)(lh2 - st4);
-      atomicMin(&ev.best[sl], key);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(kFull, best, o);
+      best = other < best ? other : best;
+    }
+    if (lane == 0 && best != ~0ull) {   // Kernel.cl:550-567
+      const uint32_t e = (uint32_t)(best >> 14) & 0x3fffu;
+      const uint32_t h1 = (uint32_t)(st1 + (int)f1) + e;
+      const uint32_t h2 = (uint32_t)st4 + (uint32_t)(best & 0x3fffu);
+      const uint32_t tp = atomicAdd(&s.ntracklets, 1u);
+      if (tp < ev.cap) {
+        ev.tracklets[tp] = make_uint4((uint32_t)h0, h1, h2, 0u);
+        push_back(s, ev, nb, kTrackletFlag | tp);
+      }
     }
   }
   if (degenerate) atomicOr(&s.status, VELO_EVENT_DEGENERATE);
-  __syncthreads();
-
-  // S5: emit one tracklet per h0 with an accepted triplet (Kernel.cl:550-567)
-  for (int sl = tid; sl < nslots; sl += nt) {
-    const unsigned long long key = ev.best[sl];
-    if (key == ~0ull) continue;
-    const int h0 = ev.slot_h0[sl];
-    const uint32_t e = (uint32_t)(key >> 14) & 0x3fffu;
-    const uint32_t h1 = (uint32_t)(ev.h1f[h0] + (int)e);
-    const uint32_t h2 = (uint32_t)st4 + (uint32_t)(key & 0x3fffu);
-    const uint32_t tp = atomicAdd(&s.ntracklets, 1u);
-    if (tp >= ev.cap) continue;
-    ev.tracklets[3 * tp + 0] = (uint32_t)h0;
-    ev.tracklets[3 * tp + 1] = h1;
-    ev.tracklets[3 * tp + 2] = h2;
-    push_ring(s, ev, nxt, kTrackletFlag | tp);
-  }
 }
+
+// Per-phase cycle counters, compiled in only with -DVELO_PHASE_CLOCKS
+// (diagnostic builds): thread 0 of every CTA adds the clock64() time between
+// the barriers that close each phase; slot 7 counts events.
+#ifdef VELO_PHASE_CLOCKS
+__device__ unsigned long long g_phase_cycles[8];
+#define VELO_PHASE_BEGIN() long long ph_t = clock64(); unsigned long long ph[7] = {0, 0, 0, 0, 0, 0, 0}
+#define VELO_PHASE(k)                 \
+  do {                                \
+    const long long t_ = clock64();   \
+    ph[k] += (unsigned long long)(t_ - ph_t); \
+    ph_t = t_;                        \
+  } while (0)
+#define VELO_PHASE_END()                                              \
+  do {                                                                \
+    if (threadIdx.x == 0) {                                           \
+      for (int k_ = 0; k_ < 7; ++k_) atomicAdd(&g_phase_cycles[k_], ph[k_]); \
+      atomicAdd(&g_phase_cycles[7], 1ull);                            \
+    }                                                                 \
+  } while (0)
+#else
+#define VELO_PHASE_BEGIN() do {} while (0)
+#define VELO_PHASE(k) do {} while (0)
+#define VELO_PHASE_END() do {} while (0)
+#endif
 
 // ---------------------------------------------------------------------------
 __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* dyn) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  VELO_PHASE_BEGIN();
   if (!p.ev_valid[e]) {
     if (tid == 0) {
       p.out_counts[e] = 0;
@@ -442,19 +505,12 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   ev.x = reinterpret_cast<float*>(arena + L.x);
   ev.y = reinterpret_cast<float*>(arena + L.y);
   ev.z = reinterpret_cast<float*>(arena + L.z);
-  ev.h1f = reinterpret_cast<int32_t*>(arena + L.h1f);
-  ev.h1l = reinterpret_cast<int32_t*>(arena + L.h1l);
-  ev.h2f = reinterpret_cast<int32_t*>(arena + L.h2f);
-  ev.h2l = reinterpret_cast<int32_t*>(arena + L.h2l);
+  ev.win = reinterpret_cast<uint2*>(arena + L.win);
   ev.used = arena + L.used;
   ev.ring0 = reinterpret_cast<uint32_t*>(arena + L.ring0);
   ev.ring1 = reinterpret_cast<uint32_t*>(arena + L.ring1);
-  ev.slot_h0 = reinterpret_cast<int32_t*>(arena + L.slot_h0);
-  ev.slot_pref = reinterpret_cast<uint32_t*>(arena + L.slot_pref);
-  ev.cutoff = reinterpret_cast<uint32_t*>(arena + L.cutoff);
-  ev.best = reinterpret_cast<unsigned long long*>(arena + L.best);
   const uint64_t hb = p.hit_base[e];
-  ev.tracklets = p.tracklets + 3 * hb;
+  ev.tracklets = reinterpret_cast<uint4*>(p.tracklets + 4 * hb);
   ev.weak = p.weak + hb;
   ev.tracks = p.tracks + hb;
 
@@ -474,7 +530,8 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     ev.used[i] = 0;
   }
   if (tid == 0) {
-    s.ncur = 0; s.nnext = 0; s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
+    s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
+    s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
   }
   if (__syncthreads_or(bad)) {   // coordinates must be finite (the host checks only the tables)
     if (tid == 0) {
@@ -484,6 +541,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     }
     return;
   }
+  VELO_PHASE(0);
 
   // per-module z range and x-sortedness (one warp per module)
   for (int m = warp; m < S; m += nwarps) {
@@ -498,22 +556,21 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
-      zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
+      zmn = fminf(zmn, __shfl_xor_sync(kFull, zmn, o));
+      zmx = fmaxf(zmx, __shfl_xor_sync(kFull, zmx, o));
     }
-    sorted = __all_sync(0xffffffffu, sorted);
+    sorted = __all_sync(kFull, sorted);
     if (lane == 0) {
       s.zmin[m] = zmn;
       s.zmax[m] = zmx;
       s.sorted[m] = sorted ? 1 : 0;
     }
   }
-  // windows of modules 0..3 stay -1 (Kernel.cl:104 gates the body on f >= 4)
+  // windows of modules 0..3 stay empty (Kernel.cl:104 gates the body on f >= 4)
   const int hbeg = S >= 5 ? s.start[4] : H;
-  for (int i = tid; i < hbeg; i += nt) {
-    ev.h1f[i] = -1; ev.h1l[i] = -1; ev.h2f[i] = -1; ev.h2l[i] = -1;
-  }
+  for (int i = tid; i < hbeg; i += nt) ev.win[i] = make_uint2(0xffffffffu, 0xffffffffu);
   __syncthreads();
+  VELO_PHASE(1);
 
   // candidate windows for every hit of modules >= 4
   for (int h = hbeg + tid; h < H; h += nt) {
@@ -524,35 +581,47 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     }
     compute_windows(ev, s, h, lo);
   }
+
+  // per-lane constants of the seeding ballots: lanes j < lane in the same
+  // Y-lane (j = lane mod Y), and lane mod Y
+  const uint32_t Y = (uint32_t)ev.Y;
+  uint32_t below_same_lane = 0;
+  for (int j = lane - (int)Y; j >= 0; j -= (int)Y) below_same_lane |= 1u << j;
+  const uint32_t lane_mod = (uint32_t)lane % Y;
   __syncthreads();
+  VELO_PHASE(2);
 
   // module loop, Kernel.cl:671-767
-  uint32_t* cur = ev.ring0;
-  uint32_t* nxt = ev.ring1;
+  int b = 0;   // ring[b] holds the entries to follow in this iteration
   for (int f = S - 1; f >= 4; --f) {
-    const uint32_t ncur = s.ncur;
-    for (uint32_t i = tid; i < ncur; i += nt) forward_entry(ev, s, cur[i], f - 4, nxt);
+    const uint32_t lo_n = min(s.ring_lo[b], ev.ring_cap);
+    const uint32_t ncur = min(lo_n + s.ring_hi[b], ev.ring_cap);
+    if (tid == 0 && s.ring_lo[b] + s.ring_hi[b] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
+    for (uint32_t i0 = (uint32_t)warp * 32u; i0 < ncur; i0 += (uint32_t)nt)   // warp-uniform
+      forward_warp(ev, s, b, lo_n, i0, ncur, f - 4, b ^ 1);
     __syncthreads();
-    if (tid == 0 && ncur + s.nnext > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
-    if (s.num[f] > 0) seed_module(ev, s, f, nxt);
-    __syncthreads();
+    VELO_PHASE(3);
     if (tid == 0) {
-      if (s.nnext > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
-      s.ncur = min(s.nnext, ev.ring_cap);
-      s.nnext = 0;
+      if (ncur + s.ring_lo[b ^ 1] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
+      s.ring_lo[b] = 0;   // ring[b] is refilled two iterations on
+      s.ring_hi[b] = 0;
     }
-    uint32_t* tmp = cur; cur = nxt; nxt = tmp;
+    if (s.num[f] > 0) seed_module(ev, s, f, b ^ 1, below_same_lane, lane_mod);
     __syncthreads();
+    VELO_PHASE(4);
+    b ^= 1;
   }
 
   // leftover tracklets become weak (Kernel.cl:771-792)
   {
-    const uint32_t ncur = s.ncur;
+    if (tid == 0 && s.ring_lo[b] + s.ring_hi[b] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
+    const uint32_t lo_n = min(s.ring_lo[b], ev.ring_cap);
+    const uint32_t ncur = min(lo_n + s.ring_hi[b], ev.ring_cap);
     for (uint32_t i = tid; i < ncur; i += nt) {
-      const uint32_t v = cur[i];
+      const uint32_t v = ring_entry(ev, b, lo_n, i);
       if (v & kTrackletFlag) {
         const uint32_t wi = atomicAdd(&s.nweak, 1u);
-        if (wi < ev.cap) ev.weak[wi] = v & kNumberMask;
+        if (wi < ev.cap) ev.weak[wi] = v & kEntryNumber;
       }
     }
   }
@@ -561,21 +630,22 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   {
     const uint32_t nweak = min(s.nweak, ev.cap);
     for (uint32_t i = tid; i < nweak; i += nt) {
-      const uint32_t w = ev.weak[i];
-      const uint32_t a = ev.tracklets[3 * w], b = ev.tracklets[3 * w + 1], c = ev.tracklets[3 * w + 2];
-      if (!ev.used[a] && !ev.used[b] && !ev.used[c]) {
+      const uint4 t = ev.tracklets[ev.weak[i]];
+      const uint32_t a = t.x, bb = t.y, c = t.z;
+      if (!ev.used[a] && !ev.used[bb] && !ev.used[c]) {
         const uint32_t tn = atomicAdd(&s.ntracks, 1u);
         if (tn >= ev.cap) continue;
         uint32_t* wr = reinterpret_cast<uint32_t*>(&ev.tracks[tn]);
-        wr[0] = 3; wr[1] = a; wr[2] = b; wr[3] = c;
+        wr[0] = 3; wr[1] = a; wr[2] = bb; wr[3] = c;
 #pragma unroll
         for (int k = 4; k < 25; ++k) wr[k] = 0;
       }
     }
   }
   __syncthreads();
+  VELO_PHASE(5);
 
-  // compacted output
+  // compacted output: one atomic per event reserves its range
   if (tid == 0) {
     const uint32_t cnt = min(s.ntracks, ev.cap);
     if (s.ntracks > VELO_MAX_TRACKS) s.status |= VELO_EVENT_MAX_TRACKS;
@@ -592,9 +662,15 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     uint32_t* dst = reinterpret_cast<uint32_t*>(p.out_tracks + s.out_first);
     for (uint32_t w = tid; w < words; w += nt) dst[w] = src[w];
   }
+  VELO_PHASE(6);
+  VELO_PHASE_END();
 }
 
-__global__ void __launch_bounds__(512) search_kernel(const SearchParams p) {
+// Three instantiations: up to 256 threads per CTA with registers budgeted
+// for 4 or for 5 resident CTAs per SM (velo_options.register_ctas), and
+// 512-thread CTAs.
+template <int kMaxThreads, int kMinCtas>
+__global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const SearchParams p) {
   extern __shared__ __align__(16) uint8_t dyn_smem[];
   __shared__ Shared s;
   if (!p.persistent) {
@@ -611,8 +687,18 @@ __global__ void __launch_bounds__(512) search_kernel(const SearchParams p) {
   }
 }
 
-int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream) {
-  search_kernel<<<grid, block, smem_bytes, (cudaStream_t)stream>>>(p);
+#define VELO_KERNEL_R4 search_kernel<256, 4>
+#define VELO_KERNEL_R5 search_kernel<256, 5>
+#define VELO_KERNEL_LARGE search_kernel<512, 1>
+
+int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (block > 256)
+    VELO_KERNEL_LARGE<<<grid, block, smem_bytes, st>>>(p);
+  else if (reg_ctas == 4)
+    VELO_KERNEL_R4<<<grid, block, smem_bytes, st>>>(p);
+  else
+    VELO_KERNEL_R5<<<grid, block, smem_bytes, st>>>(p);
   return (int)cudaGetLastError();
 }
 
@@ -625,14 +711,31 @@ int configure_search_kernel(uint32_t smem_bytes) {
   if (e != cudaSuccess) return (int)e;
   std::lock_guard<std::mutex> lock(mu);
   if (dev >= 0 && dev < 64 && configured[dev] >= smem_bytes) return 0;
-  e = cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  e = cudaFuncSetAttribute(VELO_KERNEL_R4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_R5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_LARGE, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = smem_bytes;
   return (int)e;
 }
 
-int search_occupancy(int block, uint32_t smem_bytes, int* ctas_per_sm) {
-  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, search_kernel, block,
-                                                            smem_bytes);
+#ifdef VELO_PHASE_CLOCKS
+// Reads and clears the per-phase cycle counters (diagnostic builds only).
+extern "C" int velo_debug_phase_cycles(unsigned long long* out) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(unsigned long long) * 8);
+  unsigned long long zero[8] = {};
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_phase_cycles, zero, sizeof zero);
+  return (int)e;
+}
+#endif
+
+int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int* ctas_per_sm) {
+  if (block > 256)
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_LARGE, block, smem_bytes);
+  if (reg_ctas == 4)
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_R4, block, smem_bytes);
+  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_R5, block, smem_bytes);
 }
 
 }  // namespace velo

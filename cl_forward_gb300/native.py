@@ -44,7 +44,7 @@ EXPORTED = [
     "velo_validate_event", "velo_sort_by_x", "velo_track_capacity", "velo_search",
     "velo_search_packed", "velo_stage", "velo_run", "velo_fetch", "velo_synchronize",
     "velo_get_stats", "velo_time_runs", "velo_host_alloc", "velo_host_free", "velo_device_sm_count",
-    "velo_search_device_static",
+    "velo_search_device_static", "velo_autotune",
 ]
 
 # limits of velo_search_device_static (include/velo_search.h)
@@ -56,7 +56,8 @@ class Options(ctypes.Structure):
     _fields_ = [("y_lanes", ctypes.c_int32), ("threads_per_event", ctypes.c_int32),
                 ("launch_mode", ctypes.c_int32), ("smem_hits", ctypes.c_int32),
                 ("narrow_windows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32 * 9)]
+                ("use_graph", ctypes.c_int32), ("register_ctas", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 8)]
 
 
 class Stats(ctypes.Structure):
@@ -116,6 +117,8 @@ def load() -> ctypes.CDLL:
     l.velo_device_sm_count.argtypes = [vp]
     l.velo_device_sm_count.restype = i32
     l.velo_search_device_static.argtypes = [vp, vp, vp, i32, u64, ctypes.c_uint32, i32, vp, u64, vp, vp, vp, vp]
+    l.velo_autotune.argtypes = [vp, ctypes.POINTER(Options), i32, ctypes.POINTER(Options),
+                                ctypes.POINTER(ctypes.c_float)]
     _lib = l
     return l
 
@@ -240,6 +243,15 @@ class Context:
         self._check(self._lib.velo_time_runs(self._h, ctypes.byref(opts), warmup, iters, int(flush_l2),
                                              ctypes.byref(ms)), "velo_time_runs")
         return float(ms.value)
+
+    def autotune(self, base: Optional[Options] = None, iters: int = 3):
+        """Fastest launch configuration for the staged events: (Options, ms)."""
+        b = base or default_options()
+        best = Options()
+        ms = ctypes.c_float()
+        self._check(self._lib.velo_autotune(self._h, ctypes.byref(b), iters, ctypes.byref(best), ctypes.byref(ms)),
+                    "velo_autotune")
+        return best, float(ms.value)
 
     def stats(self) -> Stats:
         s = Stats()

@@ -77,7 +77,9 @@ typedef struct velo_options {
   int32_t narrow_windows;     /* 1: binary-search narrowing of x windows (decisions unchanged) */
   int32_t ctas_per_sm;        /* persistent mode: resident CTAs per SM; 0 = auto */
   int32_t use_graph;          /* 1: capture the launch sequence in a CUDA graph and replay it */
-  int32_t reserved[9];
+  int32_t register_ctas;      /* 4 or 5: kernel build whose registers fit that many 256-thread
+                                 CTAs per SM (fewer registers, more CTAs); 0 = 5 */
+  int32_t reserved[8];
 } velo_options;
 
 typedef struct velo_stats {
@@ -150,6 +152,16 @@ velo_status velo_get_stats(const velo_ctx* ctx, velo_stats* stats);
 velo_status velo_time_runs(velo_ctx* ctx, const velo_options* opts, int32_t warmup, int32_t iters,
                            int32_t flush_l2, float* ms_out);
 
+/* Autotuner: times the staged events under a grid of launch configurations
+ * (threads per event {128, 256} x shared-memory tile {auto, 600, 900, 1200,
+ * 1600, 2400 hits} x register build {4, 5} x launch style {per event,
+ * persistent}), `iters` timed runs each with L2 flushed, and returns the
+ * fastest (median) in best_out, its milliseconds in best_ms_out.  Every
+ * configuration gives the same tracks; y_lanes and use_graph are taken from
+ * `base`. */
+velo_status velo_autotune(velo_ctx* ctx, const velo_options* base, int32_t iters,
+                          velo_options* best_out, float* best_ms_out);
+
 /* Pinned host memory (cudaHostAlloc), for callers without a CUDA runtime. */
 velo_status velo_host_alloc(velo_ctx* ctx, uint64_t bytes, void** ptr);
 velo_status velo_host_free(velo_ctx* ctx, void* ptr);
@@ -177,7 +189,7 @@ int32_t velo_device_sm_count(const velo_ctx* ctx);
  * total_hits + n_events <= VELO_STATIC_MAX_HIT_ROWS (total_hits = the sum of
  * the events' hit counts); track_capacity >= total_hits + n_events;
  * max_event_hits (an upper bound on any event's hit count) small enough to
- * stage the event in shared memory: 3,248 hits at Y = 4.  Events that break
+ * stage the event in shared memory: 7,731 hits.  Events that break
  * their declared bounds get VELO_EVENT_INVALID and no tracks.
  *
  * The first call on a device takes the array's device address (with that

@@ -87,6 +87,40 @@ def test_narrowing_and_global_arena(gpu_ctx, oracle_lib, narrow, smem_hits):
     assert smem_hits == 0 or gpu_ctx.stats().events_in_global > 0
 
 
+def test_register_builds_and_graph_replay(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import generator
+    blobs = _sorted(oracle_lib, generator.generate(range(650, 680))[0])
+    for regs in (4, 5):
+        _assert_same(gpu_ctx, oracle_lib, blobs, register_ctas=regs)
+        _assert_same(gpu_ctx, oracle_lib, blobs, register_ctas=regs, use_graph=1, launch_mode=1)
+
+
+def test_graph_replays_on_staged_events(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import events, generator, native
+    blobs = _sorted(oracle_lib, generator.generate(range(950, 990))[0])
+    want, _ = oracle_lib.search(blobs, 4)
+    buf, offs, sizes = events.pack_events(blobs)
+    cap = int(sum(max(int(np.frombuffer(b[4:8], "<i4")[0]), 1) for b in blobs))
+    gpu_ctx.stage(buf, offs, sizes)
+    o = native.default_options(use_graph=1)
+    for _ in range(3):                                   # capture once, replay
+        gpu_ctx.run(o)
+        tracks, counts, first, _ = gpu_ctx.fetch(len(blobs), cap)
+        for e in range(len(blobs)):
+            assert index_lists(tracks[int(first[e]):int(first[e]) + int(counts[e])]) == index_lists(want[e])
+    assert gpu_ctx.time_runs(o, warmup=1, iters=2) > 0
+
+
+def test_autotuned_options_keep_parity(gpu_ctx, oracle_lib, tmp_path):
+    from cl_forward_gb300 import autotune, events, generator, native
+    blobs = _sorted(oracle_lib, generator.generate(range(1500, 1700))[0])
+    buf, offs, sizes = events.pack_events(blobs)
+    gpu_ctx.stage(buf, offs, sizes)
+    o, info = autotune.tuned_options(gpu_ctx, len(blobs), 1100.0, iters=2, cache_path=str(tmp_path / "c.json"))
+    assert info["ms"] > 0 and o.register_ctas in (4, 5)
+    _assert_same(gpu_ctx, oracle_lib, blobs, **{k: getattr(o, k) for k in autotune.FIELDS})
+
+
 def test_unsorted_input_takes_exact_scans(gpu_ctx, oracle_lib):
     """Without the x-sort the reference's window scans still define the output."""
     from cl_forward_gb300 import generator
