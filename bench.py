@@ -5,6 +5,10 @@ Default workload: 10,000 events from seeds 1000..10999 of the synthetic VELO
 generator (the plain path at scale: one CTA per event, Y = 4, no FMA
 contraction), x-sorted by the reference sort before timing.
 
+The launch configuration is the autotuner's (velo_autotune: threads per
+event, shared-memory tile, register build, launch style; cached per workload
+shape), unless --no-autotune.  Every configuration gives the same tracks.
+
 Per step the GPU arm searches the whole batch once:
   value  device-resident: one kernel launch over events already in HBM, timed
          with CUDA events on the library's stream; L2 is flushed between steps
@@ -64,7 +68,8 @@ def parse_args():
     ap.add_argument("--no-narrow", action="store_true")
     ap.add_argument("--register-ctas", type=int, default=5, choices=[4, 5])
     ap.add_argument("--graph", action="store_true", help="replay launches from a CUDA graph")
-    ap.add_argument("--autotune", action="store_true", help="sweep launch configurations first (cached)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="use the library's default launch configuration instead of the autotuned one")
     ap.add_argument("--e2e-chunk", type=int, default=16000, help="events per end-to-end call")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -257,8 +262,7 @@ def gpu_arm(args, ranks: Ranks):
     import numpy as np
     from cl_forward_gb300 import events as E
 
-    if args.config in ("batched", "stress"):   # the batched configurations run tuned, from a graph
-        args.autotune = True
+    if args.config in ("batched", "stress"):   # the batched configurations replay a CUDA graph
         args.graph = True
     raw, truths = make_workload(args, ranks.rank)          # process pool before any GPU call
     blobs = sort_events(raw)

@@ -66,6 +66,16 @@ struct velo_ctx {
   velo_stats stats{};
   bool ran = false;
 
+  // learned seeding
+  DevBuf d_mlp;
+  bool mlp_set = false;
+  float keep_threshold = 0.f, window_margin = 0.f, min_keep_rate = 0.f;
+  // training-data dump of the next launch (velo_dump_doublets)
+  DevBuf d_dump_features, d_dump_ids;
+  uint64_t dump_capacity = 0;
+  uint32_t dump_keep = 0;
+  bool dump_armed = false;
+
   // bumped whenever buffers a captured launch refers to may have moved
   uint64_t generation = 0;
   cudaGraphExec_t graph = nullptr;
@@ -275,7 +285,8 @@ void velo_destroy(velo_ctx* c) {
   DevBuf* bufs[] = {&c->d_input, &c->d_ev_offset, &c->d_ev_hits, &c->d_ev_maxmod, &c->d_ev_valid,
                     &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_weak,
                     &c->d_tracks, &c->d_out_tracks, &c->d_out_counts, &c->d_out_first,
-                    &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush};
+                    &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush, &c->d_mlp,
+                    &c->d_dump_features, &c->d_dump_ids};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -385,7 +396,9 @@ velo_status prepare_launch(velo_ctx* c, const velo_options& o, uint32_t* smem_ou
     }
     budget = std::max(16u * 1024u, std::min(100u * 1024u, arena_layout(hq, hq, Y).total));
   }
-  const uint32_t limit = (uint32_t)std::max(0, c->max_smem_optin - 8 * 1024);
+  // room for the static shared state, and for the MLP weights ahead of the arena
+  const int reserve = 8 * 1024 + (o.learned ? (int)velo::kMlpSmemBytes : 0);
+  const uint32_t limit = (uint32_t)std::max(0, c->max_smem_optin - reserve);
   budget = std::min(budget, limit);
   uint32_t smem = 16;
   for (int32_t e = 0; e < c->n; ++e) {
@@ -455,17 +468,39 @@ velo_status check_options(velo_ctx* c, const velo_options* opts, velo_options* o
     c->err = "register_ctas must be 4 or 5";
     return VELO_ERR_INVALID_ARGUMENT;
   }
+  if (o->learned && !c->mlp_set) {
+    c->err = "learned seeding needs weights (velo_set_mlp)";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
+  if (o->learned || c->dump_armed) {
+    if (o->threads_per_event > 256) o->threads_per_event = 256;
+    o->use_graph = 0;
+  }
   return VELO_OK;
 }
 
 // Grid of the launch (the occupancy query stays outside any stream capture).
+int launch_mode_of(const velo_ctx* c, const velo_options& o) {
+  if (o.learned) return velo::kModeLearned;
+  if (c->dump_armed) return velo::kModeDump;
+  return velo::kModePlain;
+}
+
+// Dynamic shared memory of the launch: the arena, after the MLP weights when learned.
+uint32_t launch_smem(const velo_options& o, uint32_t arena_smem) {
+  return arena_smem + (o.learned ? velo::kMlpSmemBytes : 0u);
+}
+
 velo_status launch_shape(velo_ctx* c, const velo_options& o, uint32_t smem, int* grid) {
   *grid = c->n;
+  const int ce = velo::configure_search_kernel(launch_smem(o, smem));
+  if (ce != 0) return cuda_fail(c, (cudaError_t)ce, "cudaFuncSetAttribute");
   if (o.launch_mode == VELO_LAUNCH_PERSISTENT && c->n > 0) {
     int per_sm = o.ctas_per_sm;
     if (per_sm <= 0) {
       int occ = 0;
-      int e = velo::search_occupancy(o.threads_per_event, smem, o.register_ctas, &occ);
+      int e = velo::search_occupancy(o.threads_per_event, launch_smem(o, smem), o.register_ctas,
+                                     launch_mode_of(c, o), &occ);
       if (e != 0) return cuda_fail(c, (cudaError_t)e, "occupancy");
       per_sm = std::max(occ, 1);
     }
@@ -502,7 +537,20 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
   p.out_status = P<uint32_t>(c->d_out_status);
   p.out_cursor = P<unsigned long long>(c->d_counters);
   p.work_counter = reinterpret_cast<int32_t*>(P<uint8_t>(c->d_counters) + 32);
-  int e = velo::launch_search(p, grid, o.threads_per_event, smem, c->stream, o.register_ctas);
+  if (o.learned) {
+    p.mlp = P<float>(c->d_mlp);
+    p.keep_threshold = c->keep_threshold;
+    p.window_margin = c->window_margin;
+    p.min_keep_rate = c->min_keep_rate;
+  }
+  if (c->dump_armed) {
+    p.dump_features = P<float>(c->d_dump_features);
+    p.dump_ids = P<uint32_t>(c->d_dump_ids);
+    p.dump_count = reinterpret_cast<unsigned long long*>(P<uint8_t>(c->d_counters) + 40);
+    p.dump_capacity = c->dump_capacity;
+    p.dump_keep = c->dump_keep;
+  }
+  int e = velo::launch_search(p, grid, o.threads_per_event, launch_smem(o, smem), c->stream, o.register_ctas);
   if (e != 0) return cuda_fail(c, (cudaError_t)e, "search kernel launch");
   return VELO_OK;
 }
@@ -519,8 +567,8 @@ velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
   c->stats.smem_bytes_per_cta = (int32_t)smem;
   if (!o.use_graph) return enqueue_kernel(c, o, smem, grid);
   const uint64_t key[8] = {c->generation, smem, (uint64_t)grid, (uint64_t)o.threads_per_event,
-                           (uint64_t)o.register_ctas, (uint64_t)o.y_lanes, (uint64_t)o.narrow_windows,
-                           (uint64_t)o.launch_mode};
+                           (uint64_t)o.register_ctas | ((uint64_t)o.learned << 8), (uint64_t)o.y_lanes,
+                           (uint64_t)o.narrow_windows, (uint64_t)o.launch_mode};
   if (!c->graph || std::memcmp(key, c->graph_key, sizeof key) != 0) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
@@ -745,6 +793,59 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
           }
         }
   if (best_ms_out) *best_ms_out = best;
+  return VELO_OK;
+}
+
+velo_status velo_set_mlp(velo_ctx* c, const float* weights, float keep_threshold, float window_margin,
+                         float min_keep_rate) {
+  if (!c || !weights) return VELO_ERR_INVALID_ARGUMENT;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  velo_status st = ensure(c, c->d_mlp, sizeof(float) * VELO_MLP_PARAMS, "mlp");
+  if (st != VELO_OK) return st;
+  VELO_CUDA(c, cudaMemcpyAsync(c->d_mlp.p, weights, sizeof(float) * VELO_MLP_PARAMS, cudaMemcpyHostToDevice,
+                               c->stream));
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->keep_threshold = keep_threshold;
+  c->window_margin = window_margin;
+  c->min_keep_rate = min_keep_rate;
+  c->mlp_set = true;
+  return VELO_OK;
+}
+
+velo_status velo_dump_doublets(velo_ctx* c, const velo_options* opts, uint32_t keep_one_in, float* features_out,
+                               uint32_t* ids_out, uint64_t capacity, uint64_t* count_out) {
+  if (!c || (capacity && (!features_out || !ids_out))) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->staged) return VELO_ERR_NOT_STAGED;
+  velo_options o;
+  if (opts) o = *opts; else velo_default_options(&o);
+  o.learned = 0;   // the training data comes from the plain method
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  velo_status st;
+  if ((st = ensure(c, c->d_dump_features, sizeof(float) * VELO_MLP_INPUTS * (capacity ? capacity : 1),
+                   "dump features")) != VELO_OK)
+    return st;
+  if ((st = ensure(c, c->d_dump_ids, sizeof(uint32_t) * 3 * (capacity ? capacity : 1), "dump ids")) != VELO_OK)
+    return st;
+  c->dump_capacity = capacity;
+  c->dump_keep = keep_one_in ? keep_one_in : 1u;
+  c->dump_armed = true;
+  c->generation++;
+  st = velo_run(c, &o);
+  c->dump_armed = false;
+  c->generation++;
+  if (st != VELO_OK) return st;
+  uint64_t count = 0;
+  VELO_CUDA(c, cudaMemcpyAsync(&count, P<uint8_t>(c->d_counters) + 40, 8, cudaMemcpyDeviceToHost, c->stream));
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  const uint64_t k = count < capacity ? count : capacity;
+  if (k) {
+    VELO_CUDA(c, cudaMemcpyAsync(features_out, c->d_dump_features.p, sizeof(float) * VELO_MLP_INPUTS * k,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    VELO_CUDA(c, cudaMemcpyAsync(ids_out, c->d_dump_ids.p, sizeof(uint32_t) * 3 * k, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  if (count_out) *count_out = count;
   return VELO_OK;
 }
 

@@ -30,6 +30,20 @@ constexpr uint32_t kTrackletFlag = 0x80000000u;
 constexpr uint32_t kSkipMask = 0x70000000u;
 constexpr uint64_t kNoArena = ~0ull;
 
+// MLP parameter layout (velo_search.h): W1[32][10] b1[32] W2[32][32] b2[32]
+// W3[2][32] b3[2]
+constexpr int kMlpIn = VELO_MLP_INPUTS;
+constexpr int kMlpHidden = VELO_MLP_HIDDEN;
+constexpr int kMlpOut = VELO_MLP_OUTPUTS;
+constexpr int kMlpW1 = 0;
+constexpr int kMlpB1 = kMlpW1 + kMlpHidden * kMlpIn;
+constexpr int kMlpW2 = kMlpB1 + kMlpHidden;
+constexpr int kMlpB2 = kMlpW2 + kMlpHidden * kMlpHidden;
+constexpr int kMlpW3 = kMlpB2 + kMlpHidden;
+constexpr int kMlpB3 = kMlpW3 + kMlpOut * kMlpHidden;
+static_assert(kMlpB3 + kMlpOut == VELO_MLP_PARAMS, "MLP parameter count");
+constexpr uint32_t kMlpSmemBytes = (VELO_MLP_PARAMS * 4 + 15) & ~15;
+
 // Per-event working set ("arena"): staged in dynamic shared memory when it
 // fits the launch's shared-memory size, else carved from global scratch.
 // Offsets are bytes, each array 16-byte aligned.  29 bytes per hit.
@@ -88,6 +102,17 @@ struct SearchParams {
   uint32_t* out_status;
   unsigned long long* out_cursor; // running total of compacted tracks
   int32_t* work_counter;          // persistent mode queue head
+  // training data: features and {event, h0, h1} of sampled doublets
+  float* dump_features;
+  uint32_t* dump_ids;
+  unsigned long long* dump_count;
+  uint64_t dump_capacity;
+  uint32_t dump_keep;             // one in dump_keep doublets (hash-sampled)
+  // learned seeding: MLP weights (null = plain), prefix of the dynamic shared memory
+  const float* mlp;
+  float keep_threshold;
+  float window_margin;
+  float min_keep_rate;
 };
 
 // Launches the search kernel (velo_kernels.cu); reg_ctas (4 or 5) picks the
@@ -96,6 +121,8 @@ int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_byte
 // Sets the kernels' maximum dynamic shared memory.  Returns a cudaError_t value.
 int configure_search_kernel(uint32_t smem_bytes);
 // Maximum resident CTAs per SM for a block size, shared-memory size and build.
-int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int* ctas_per_sm);
+int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, int* ctas_per_sm);
+// kernel modes (velo_kernels.cu): plain, plain + training-data dump, learned
+constexpr int kModePlain = 0, kModeDump = 1, kModeLearned = 2;
 
 }  // namespace velo

@@ -60,6 +60,7 @@ struct Shared {
   uint32_t ring_lo[2];   // forwarding entries, from the front of ring[i]
   uint32_t ring_hi[2];   // seeding entries, from the back of ring[i]
   uint32_t ntracks, ntracklets, nweak, status;
+  uint32_t considered, kept;   // learned seeding: doublets scored / kept
   unsigned long long out_first;
   int32_t next_event;
 };
@@ -77,6 +78,14 @@ struct EventView {
   uint32_t* weak;
   velo_track* tracks;
   bool narrow;
+  int event;
+  const float* mlp;         // learned seeding: weights in shared memory
+  float keep_threshold, window_margin;
+  float* dump_features;     // training-data dump
+  uint32_t* dump_ids;
+  unsigned long long* dump_count;
+  uint64_t dump_capacity;
+  uint32_t dump_keep;
 };
 
 // First index i in [lo, hi) with x[i] > c, for non-decreasing x.
@@ -336,10 +345,61 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
   if (action == kWeak && wi < ev.cap) ev.weak[wi] = trackno;
 }
 
+// Features of an (h0, h1) doublet seen by the learned seeding (and recorded
+// as training data): slopes, h0 radius and azimuth, module, predicted x / y
+// at module f-4, z gap, h2 candidates in the exact window, and the y-slope
+// cut margin.  Plain FP32; the features steer pruning, not the cuts.
+__device__ __forceinline__ void doublet_features(float* f, float h0x, float h0y, float h0z, float h1x, float h1y,
+                                                 float h1z, int module, int n_modules, float zmid4, int h2_window,
+                                                 float dymax) {
+  const float dz = h1z - h0z;
+  const float inv = 1.f / dz;
+  const float tx = (h1x - h0x) * inv, ty = (h1y - h0y) * inv;
+  f[0] = 5.f * tx;
+  f[1] = 5.f * ty;
+  f[2] = sqrtf(h0x * h0x + h0y * h0y) * (1.f / 42.f);
+  f[3] = atan2f(h0y, h0x) * 0.31830988f;
+  f[4] = (float)module / (float)n_modules;
+  f[5] = (h0x + tx * (zmid4 - h0z)) * (1.f / 42.f);
+  f[6] = (h0y + ty * (zmid4 - h0z)) * (1.f / 42.f);
+  f[7] = dz * 0.01f;
+  f[8] = (float)h2_window * (1.f / 32.f);
+  f[9] = fabsf(h1y - h0y) / dymax;
+}
+
+// The 10 -> 32 -> 32 -> 2 MLP on one doublet, weights in shared memory.
+__device__ __forceinline__ void mlp_eval(const float* __restrict__ w, const float* x, float* logit, float* width) {
+  float a1[kMlpHidden];
+#pragma unroll
+  for (int j = 0; j < kMlpHidden; ++j) {
+    float acc = w[kMlpB1 + j];
+#pragma unroll
+    for (int i = 0; i < kMlpIn; ++i) acc += w[kMlpW1 + j * kMlpIn + i] * x[i];
+    a1[j] = fmaxf(acc, 0.f);
+  }
+  float z = w[kMlpB3], wd = w[kMlpB3 + 1];
+#pragma unroll 4
+  for (int j = 0; j < kMlpHidden; ++j) {
+    float acc = w[kMlpB2 + j];
+#pragma unroll
+    for (int i = 0; i < kMlpHidden; ++i) acc += w[kMlpW2 + j * kMlpHidden + i] * a1[i];
+    acc = fmaxf(acc, 0.f);
+    z += w[kMlpW3 + j] * acc;
+    wd += w[kMlpW3 + kMlpHidden + j] * acc;
+  }
+  *logit = z;
+  *width = wd;
+}
+
+constexpr int kPlain = 0;    // the reference's seeding
+constexpr int kDump = 1;     // plain, recording sampled doublets as training data
+constexpr int kLearned = 2;  // MLP-pruned seeding
+
 // Seeding of module f: h0 on f, h1 on f-2, h2 on f-4 (Kernel.cl:392-568
 // with the unused-h0 gather of :720-764).  One warp per h0; lane j of chunk c
 // takes h1 element e = 32c + j, which belongs to the reference's Y-lane
 // e mod Y.  New tracklets go to the back of ring[nb].
+template <int kMode>
 __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint32_t below_same_lane,
                             uint32_t lane_mod) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -382,18 +442,61 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
       dead_lanes |= __reduce_or_sync(kFull, dead ? (1u << ly) : 0u);
       chunk_mod += chunk_step;
       if (chunk_mod >= Y) chunk_mod -= Y;
-      if (!in || dead || stopped || ev.used[h1]) continue;
-      const float h1x = ev.x[h1], h1y = ev.y[h1], h1z = ev.z[h1];
-      if (!(fabsf(fsub(h1y, h0y)) < dymax)) continue;   // h2-independent term of Kernel.cl:509
+      bool cand = in && !dead && !stopped && !ev.used[h1];
+      float h1x = 0.f, h1y = 0.f, h1z = 0.f;
+      if (cand) {
+        h1x = ev.x[h1];
+        h1y = ev.y[h1];
+        h1z = ev.z[h1];
+        cand = fabsf(fsub(h1y, h0y)) < dymax;        // h2-independent term of Kernel.cl:509
+      }
+      int a = (int)(w1 & 0xffffu), b = (int)(w1 >> 16);
+      float tol = kTolerance;
+      if constexpr (kMode != kPlain) {
+        bool keep = cand;
+        if (cand) {
+          float feat[kMlpIn];
+          doublet_features(feat, h0x, h0y, h0z, h1x, h1y, h1z, f, ev.S, 0.5f * (zmin4 + zmax4), b - a, dymax);
+          if constexpr (kMode == kDump) {
+            uint32_t hs = (uint32_t)ev.event * 0x9E3779B1u ^ (uint32_t)h0 * 0x85EBCA77u ^ (uint32_t)h1 * 0xC2B2AE3Du;
+            hs ^= hs >> 15;
+            hs *= 0x2C1B3C6Du;
+            hs ^= hs >> 12;
+            if (hs % ev.dump_keep == 0u) {
+              const unsigned long long k = atomicAdd(ev.dump_count, 1ull);
+              if (k < ev.dump_capacity) {
+#pragma unroll
+                for (int q = 0; q < kMlpIn; ++q) ev.dump_features[k * kMlpIn + q] = feat[q];
+                ev.dump_ids[3 * k + 0] = (uint32_t)ev.event;
+                ev.dump_ids[3 * k + 1] = (uint32_t)h0;
+                ev.dump_ids[3 * k + 2] = (uint32_t)h1;
+              }
+            }
+          } else {
+            float logit, width;
+            mlp_eval(ev.mlp, feat, &logit, &width);
+            keep = logit >= ev.keep_threshold;
+            tol = fminf(kTolerance, fmaxf(width, 0.f) + ev.window_margin);
+          }
+        }
+        if constexpr (kMode == kLearned) {           // keep-rate bookkeeping for the guard
+          const unsigned mc = __ballot_sync(kFull, cand), mk = __ballot_sync(kFull, cand && keep);
+          if (lane == 0 && mc) {
+            atomicAdd(&s.considered, (uint32_t)__popc(mc));
+            atomicAdd(&s.kept, (uint32_t)__popc(mk));
+          }
+          cand = cand && keep;
+        }
+      }
+      if (!cand) continue;
       const float dz_inverted = fdiv(1.f, fsub(h1z, h0z));
       const float ddx = fsub(h1x, h0x), ddy = fsub(h1y, h0y);
-      int a = (int)(w1 & 0xffffu), b = (int)(w1 >> 16);
       if (narrow4) {
         const float xa = fadd(h0x, fmul(ddx, fmul(fsub(zmin4, h0z), dz_inverted)));
         const float xb = fadd(h0x, fmul(ddx, fmul(fsub(zmax4, h0z), dz_inverted)));
         if (isfinite(xa) && isfinite(xb) && a < b) {
           int lo, hi;
-          narrow_range(x4, a, b, fminf(xa, xb), fmaxf(xa, xb), kTolerance, &lo, &hi);
+          narrow_range(x4, a, b, fminf(xa, xb), fmaxf(xa, xb), tol, &lo, &hi);
           a = lo;
           b = hi;
         }
@@ -472,7 +575,8 @@ __device__ unsigned long long g_phase_cycles[8];
 #endif
 
 // ---------------------------------------------------------------------------
-__device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* dyn) {
+template <int kMode>
+__device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* dyn, const float* mlp_smem) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   VELO_PHASE_BEGIN();
@@ -513,6 +617,15 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   ev.tracklets = reinterpret_cast<uint4*>(p.tracklets + 4 * hb);
   ev.weak = p.weak + hb;
   ev.tracks = p.tracks + hb;
+  ev.event = e;
+  ev.mlp = mlp_smem;
+  ev.keep_threshold = p.keep_threshold;
+  ev.window_margin = p.window_margin;
+  ev.dump_features = p.dump_features;
+  ev.dump_ids = p.dump_ids;
+  ev.dump_count = p.dump_count;
+  ev.dump_capacity = p.dump_capacity;
+  ev.dump_keep = p.dump_keep > 0 ? p.dump_keep : 1u;
 
   // stage the event
   for (int m = tid; m < S; m += nt) {
@@ -532,6 +645,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   if (tid == 0) {
     s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
     s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
+    s.considered = 0; s.kept = 0;
   }
   if (__syncthreads_or(bad)) {   // coordinates must be finite (the host checks only the tables)
     if (tid == 0) {
@@ -591,59 +705,85 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   __syncthreads();
   VELO_PHASE(2);
 
-  // module loop, Kernel.cl:671-767
-  int b = 0;   // ring[b] holds the entries to follow in this iteration
-  for (int f = S - 1; f >= 4; --f) {
-    const uint32_t lo_n = min(s.ring_lo[b], ev.ring_cap);
-    const uint32_t ncur = min(lo_n + s.ring_hi[b], ev.ring_cap);
-    if (tid == 0 && s.ring_lo[b] + s.ring_hi[b] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
-    for (uint32_t i0 = (uint32_t)warp * 32u; i0 < ncur; i0 += (uint32_t)nt)   // warp-uniform
-      forward_warp(ev, s, b, lo_n, i0, ncur, f - 4, b ^ 1);
-    __syncthreads();
-    VELO_PHASE(3);
-    if (tid == 0) {
-      if (ncur + s.ring_lo[b ^ 1] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
-      s.ring_lo[b] = 0;   // ring[b] is refilled two iterations on
-      s.ring_hi[b] = 0;
+  // The learned seeding runs first when enabled; if it kept too small a
+  // fraction of the doublets it scored, the event is searched again by the
+  // plain method (used flags and lists reset; windows kept).
+  bool learned = kMode == kLearned;
+  uint32_t fallback = 0;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if (attempt > 0) {
+      for (int i = tid; i < H; i += nt) ev.used[i] = 0;
+      if (tid == 0) {
+        s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
+        s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
+      }
+      __syncthreads();
     }
-    if (s.num[f] > 0) seed_module(ev, s, f, b ^ 1, below_same_lane, lane_mod);
-    __syncthreads();
-    VELO_PHASE(4);
-    b ^= 1;
-  }
+    // module loop, Kernel.cl:671-767
+    int b = 0;   // ring[b] holds the entries to follow in this iteration
+    for (int f = S - 1; f >= 4; --f) {
+      const uint32_t lo_n = min(s.ring_lo[b], ev.ring_cap);
+      const uint32_t ncur = min(lo_n + s.ring_hi[b], ev.ring_cap);
+      if (tid == 0 && s.ring_lo[b] + s.ring_hi[b] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
+      for (uint32_t i0 = (uint32_t)warp * 32u; i0 < ncur; i0 += (uint32_t)nt)   // warp-uniform
+        forward_warp(ev, s, b, lo_n, i0, ncur, f - 4, b ^ 1);
+      __syncthreads();
+      VELO_PHASE(3);
+      if (tid == 0) {
+        if (ncur + s.ring_lo[b ^ 1] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
+        s.ring_lo[b] = 0;   // ring[b] is refilled two iterations on
+        s.ring_hi[b] = 0;
+      }
+      if (s.num[f] > 0) {
+        if (learned)
+          seed_module<kLearned>(ev, s, f, b ^ 1, below_same_lane, lane_mod);
+        else
+          seed_module<kMode == kDump ? kDump : kPlain>(ev, s, f, b ^ 1, below_same_lane, lane_mod);
+      }
+      __syncthreads();
+      VELO_PHASE(4);
+      b ^= 1;
+    }
 
-  // leftover tracklets become weak (Kernel.cl:771-792)
-  {
-    if (tid == 0 && s.ring_lo[b] + s.ring_hi[b] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
-    const uint32_t lo_n = min(s.ring_lo[b], ev.ring_cap);
-    const uint32_t ncur = min(lo_n + s.ring_hi[b], ev.ring_cap);
-    for (uint32_t i = tid; i < ncur; i += nt) {
-      const uint32_t v = ring_entry(ev, b, lo_n, i);
-      if (v & kTrackletFlag) {
-        const uint32_t wi = atomicAdd(&s.nweak, 1u);
-        if (wi < ev.cap) ev.weak[wi] = v & kEntryNumber;
+    // leftover tracklets become weak (Kernel.cl:771-792)
+    {
+      if (tid == 0 && s.ring_lo[b] + s.ring_hi[b] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
+      const uint32_t lo_n = min(s.ring_lo[b], ev.ring_cap);
+      const uint32_t ncur = min(lo_n + s.ring_hi[b], ev.ring_cap);
+      for (uint32_t i = tid; i < ncur; i += nt) {
+        const uint32_t v = ring_entry(ev, b, lo_n, i);
+        if (v & kTrackletFlag) {
+          const uint32_t wi = atomicAdd(&s.nweak, 1u);
+          if (wi < ev.cap) ev.weak[wi] = v & kEntryNumber;
+        }
       }
     }
-  }
-  __syncthreads();
-  // weak tracks made of three unused hits (Kernel.cl:796-815)
-  {
-    const uint32_t nweak = min(s.nweak, ev.cap);
-    for (uint32_t i = tid; i < nweak; i += nt) {
-      const uint4 t = ev.tracklets[ev.weak[i]];
-      const uint32_t a = t.x, bb = t.y, c = t.z;
-      if (!ev.used[a] && !ev.used[bb] && !ev.used[c]) {
-        const uint32_t tn = atomicAdd(&s.ntracks, 1u);
-        if (tn >= ev.cap) continue;
-        uint32_t* wr = reinterpret_cast<uint32_t*>(&ev.tracks[tn]);
-        wr[0] = 3; wr[1] = a; wr[2] = bb; wr[3] = c;
-#pragma unroll
-        for (int k = 4; k < 25; ++k) wr[k] = 0;
+    __syncthreads();
+    // weak tracks made of three unused hits (Kernel.cl:796-815)
+    {
+      const uint32_t nweak = min(s.nweak, ev.cap);
+      for (uint32_t i = tid; i < nweak; i += nt) {
+        const uint4 t = ev.tracklets[ev.weak[i]];
+        const uint32_t a = t.x, bb = t.y, c = t.z;
+        if (!ev.used[a] && !ev.used[bb] && !ev.used[c]) {
+          const uint32_t tn = atomicAdd(&s.ntracks, 1u);
+          if (tn >= ev.cap) continue;
+          uint32_t* wr = reinterpret_cast<uint32_t*>(&ev.tracks[tn]);
+          wr[0] = 3; wr[1] = a; wr[2] = bb; wr[3] = c;
+  #pragma unroll
+          for (int k = 4; k < 25; ++k) wr[k] = 0;
+        }
       }
     }
+    __syncthreads();
+    VELO_PHASE(5);
+    if (!learned) break;
+    const uint32_t considered = s.considered, kept = s.kept;   // final after the barrier above
+    if (considered == 0 || (float)kept >= p.min_keep_rate * (float)considered) break;
+    learned = false;
+    fallback = VELO_EVENT_LEARNED_FALLBACK;
+    __syncthreads();   // everyone has read the counters before the reset
   }
-  __syncthreads();
-  VELO_PHASE(5);
 
   // compacted output: one atomic per event reserves its range
   if (tid == 0) {
@@ -653,7 +793,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     s.out_first = first;
     p.out_counts[e] = cnt;
     p.out_first[e] = first;
-    p.out_status[e] = s.status;
+    p.out_status[e] = s.status | fallback;
   }
   __syncthreads();
   {
@@ -669,12 +809,22 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
 // Three instantiations: up to 256 threads per CTA with registers budgeted
 // for 4 or for 5 resident CTAs per SM (velo_options.register_ctas), and
 // 512-thread CTAs.
-template <int kMaxThreads, int kMinCtas>
+template <int kMaxThreads, int kMinCtas, int kMode>
 __global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const SearchParams p) {
-  extern __shared__ __align__(16) uint8_t dyn_smem[];
+  extern __shared__ __align__(16) uint8_t dyn_smem_raw[];
   __shared__ Shared s;
+  // learned seeding: the MLP weights lead the dynamic shared memory
+  const float* mlp_smem = nullptr;
+  uint8_t* dyn_smem = dyn_smem_raw;
+  if constexpr (kMode == kLearned) {
+    float* w = reinterpret_cast<float*>(dyn_smem_raw);
+    for (int i = threadIdx.x; i < VELO_MLP_PARAMS; i += blockDim.x) w[i] = p.mlp[i];
+    __syncthreads();
+    mlp_smem = w;
+    dyn_smem = dyn_smem_raw + kMlpSmemBytes;
+  }
   if (!p.persistent) {
-    if ((int)blockIdx.x < p.n_events) process_event(p, blockIdx.x, s, dyn_smem);
+    if ((int)blockIdx.x < p.n_events) process_event<kMode>(p, blockIdx.x, s, dyn_smem, mlp_smem);
     return;
   }
   for (;;) {
@@ -683,17 +833,23 @@ __global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const Sea
     __syncthreads();
     const int k = s.next_event;
     if (k >= p.n_events) break;
-    process_event(p, p.order[k], s, dyn_smem);
+    process_event<kMode>(p, p.order[k], s, dyn_smem, mlp_smem);
   }
 }
 
-#define VELO_KERNEL_R4 search_kernel<256, 4>
-#define VELO_KERNEL_R5 search_kernel<256, 5>
-#define VELO_KERNEL_LARGE search_kernel<512, 1>
+#define VELO_KERNEL_R4 search_kernel<256, 4, kPlain>
+#define VELO_KERNEL_R5 search_kernel<256, 5, kPlain>
+#define VELO_KERNEL_LARGE search_kernel<512, 1, kPlain>
+#define VELO_KERNEL_DUMP search_kernel<256, 4, kDump>
+#define VELO_KERNEL_LEARNED search_kernel<256, 4, kLearned>
 
 int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas) {
   cudaStream_t st = (cudaStream_t)stream;
-  if (block > 256)
+  if (p.mlp)
+    VELO_KERNEL_LEARNED<<<grid, min(block, 256), smem_bytes, st>>>(p);
+  else if (p.dump_features)
+    VELO_KERNEL_DUMP<<<grid, min(block, 256), smem_bytes, st>>>(p);
+  else if (block > 256)
     VELO_KERNEL_LARGE<<<grid, block, smem_bytes, st>>>(p);
   else if (reg_ctas == 4)
     VELO_KERNEL_R4<<<grid, block, smem_bytes, st>>>(p);
@@ -716,6 +872,10 @@ int configure_search_kernel(uint32_t smem_bytes) {
     e = cudaFuncSetAttribute(VELO_KERNEL_R5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(VELO_KERNEL_LARGE, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_DUMP, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_LEARNED, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = smem_bytes;
   return (int)e;
 }
@@ -730,7 +890,13 @@ extern "C" int velo_debug_phase_cycles(unsigned long long* out) {
 }
 #endif
 
-int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int* ctas_per_sm) {
+int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, int* ctas_per_sm) {
+  if (mode == kLearned)
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_LEARNED, min(block, 256),
+                                                              smem_bytes);
+  if (mode == kDump)
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_DUMP, min(block, 256),
+                                                              smem_bytes);
   if (block > 256)
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_LARGE, block, smem_bytes);
   if (reg_ctas == 4)

@@ -44,8 +44,14 @@ EXPORTED = [
     "velo_validate_event", "velo_sort_by_x", "velo_track_capacity", "velo_search",
     "velo_search_packed", "velo_stage", "velo_run", "velo_fetch", "velo_synchronize",
     "velo_get_stats", "velo_time_runs", "velo_host_alloc", "velo_host_free", "velo_device_sm_count",
-    "velo_search_device_static", "velo_autotune",
+    "velo_search_device_static", "velo_autotune", "velo_set_mlp", "velo_dump_doublets",
+    "velo_mlp_train", "velo_mlp_grad", "velo_mlp_forward",
 ]
+
+MLP_INPUTS = 10
+MLP_HIDDEN = 32
+MLP_PARAMS = 1474
+EVENT_LEARNED_FALLBACK = 0x20
 
 # limits of velo_search_device_static (include/velo_search.h)
 STATIC_MAX_EVENTS = 4096
@@ -57,7 +63,7 @@ class Options(ctypes.Structure):
                 ("launch_mode", ctypes.c_int32), ("smem_hits", ctypes.c_int32),
                 ("narrow_windows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("register_ctas", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 8)]
+                ("learned", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
 
 
 class Stats(ctypes.Structure):
@@ -119,6 +125,13 @@ def load() -> ctypes.CDLL:
     l.velo_search_device_static.argtypes = [vp, vp, vp, i32, u64, ctypes.c_uint32, i32, vp, u64, vp, vp, vp, vp]
     l.velo_autotune.argtypes = [vp, ctypes.POINTER(Options), i32, ctypes.POINTER(Options),
                                 ctypes.POINTER(ctypes.c_float)]
+    f32 = ctypes.c_float
+    l.velo_set_mlp.argtypes = [vp, vp, f32, f32, f32]
+    l.velo_dump_doublets.argtypes = [vp, ctypes.POINTER(Options), ctypes.c_uint32, vp, vp, u64,
+                                     ctypes.POINTER(u64)]
+    l.velo_mlp_train.argtypes = [vp, vp, vp, ctypes.c_int64, i32, i32, f32, u64, vp, vp]
+    l.velo_mlp_grad.argtypes = [vp, vp, vp, vp, ctypes.c_int64, vp, ctypes.POINTER(f32)]
+    l.velo_mlp_forward.argtypes = [vp, vp, ctypes.c_int64, vp]
     _lib = l
     return l
 
@@ -253,6 +266,23 @@ class Context:
                     "velo_autotune")
         return best, float(ms.value)
 
+    def set_mlp(self, weights: np.ndarray, keep_threshold: float, window_margin: float, min_keep_rate: float):
+        w = np.ascontiguousarray(weights, np.float32)
+        assert w.size == MLP_PARAMS
+        self._check(self._lib.velo_set_mlp(self._h, _p(w), keep_threshold, window_margin, min_keep_rate),
+                    "velo_set_mlp")
+
+    def dump_doublets(self, capacity: int, keep_one_in: int = 1, options: Optional[Options] = None):
+        """Features and {event, h0, h1} of sampled doublets of a plain run on the staged events."""
+        feats = np.zeros((max(capacity, 1), MLP_INPUTS), np.float32)
+        ids = np.zeros((max(capacity, 1), 3), np.uint32)
+        count = ctypes.c_uint64()
+        opts = options or default_options()
+        self._check(self._lib.velo_dump_doublets(self._h, ctypes.byref(opts), keep_one_in, _p(feats), _p(ids),
+                                                 capacity, ctypes.byref(count)), "velo_dump_doublets")
+        k = min(int(count.value), capacity)
+        return feats[:k], ids[:k], int(count.value)
+
     def stats(self) -> Stats:
         s = Stats()
         self._check(self._lib.velo_get_stats(self._h, ctypes.byref(s)), "velo_get_stats")
@@ -270,3 +300,41 @@ class Context:
 
     def host_free(self, arr: np.ndarray):
         self._check(self._lib.velo_host_free(self._h, ctypes.c_void_p(arr.ctypes.data)), "velo_host_free")
+
+
+def _check_free(st: int, what: str):
+    if st != OK:
+        raise VeloError(st, f"{what}: {load().velo_status_string(st).decode()}")
+
+
+def mlp_train(x: np.ndarray, label: np.ndarray, target: np.ndarray, weights: np.ndarray, steps: int,
+              batch: int = 4096, lr: float = 1e-3, seed: int = 0):
+    """Adam training with the library's CUDA kernels; returns (weights, loss per step)."""
+    x = np.ascontiguousarray(x, np.float32)
+    label = np.ascontiguousarray(label, np.float32)
+    target = np.ascontiguousarray(target, np.float32)
+    w = np.ascontiguousarray(weights, np.float32).copy()
+    loss = np.zeros(steps, np.float32)
+    _check_free(load().velo_mlp_train(_p(x), _p(label), _p(target), len(x), steps, batch, lr, seed, _p(w), _p(loss)),
+                "velo_mlp_train")
+    return w, loss
+
+
+def mlp_grad(weights: np.ndarray, x: np.ndarray, label: np.ndarray, target: np.ndarray):
+    w = np.ascontiguousarray(weights, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    label = np.ascontiguousarray(label, np.float32)
+    target = np.ascontiguousarray(target, np.float32)
+    g = np.zeros(MLP_PARAMS, np.float32)
+    loss = ctypes.c_float()
+    _check_free(load().velo_mlp_grad(_p(w), _p(x), _p(label), _p(target), len(x), _p(g), ctypes.byref(loss)),
+                "velo_mlp_grad")
+    return g, float(loss.value)
+
+
+def mlp_forward(weights: np.ndarray, x: np.ndarray) -> np.ndarray:
+    w = np.ascontiguousarray(weights, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros((len(x), 2), np.float32)
+    _check_free(load().velo_mlp_forward(_p(w), _p(x), len(x), _p(out)), "velo_mlp_forward")
+    return out

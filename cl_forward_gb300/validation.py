@@ -128,3 +128,51 @@ def rates(all_tracks: Iterable[np.ndarray], blobs: Sequence[bytes], truths: Sequ
     for t, b, tr in zip(all_tracks, blobs, truths):
         total.add(event_rates(t, b, tr))
     return total
+
+
+def event_rates_fast(tracks: np.ndarray, hit_id: np.ndarray, truth: Truth, min_hits: int = 3) -> Rates:
+    """Vectorised :func:`event_rates` (same definitions), for large batches."""
+    r = Rates()
+    recon = truth.n_hits >= min_hits
+    low = truth.p < 2.0
+    r.reconstructible = int(recon.sum())
+    r.recon_low = int((recon & low).sum())
+    r.recon_high = int((recon & ~low).sum())
+    T = len(tracks)
+    r.tracks = T
+    if T == 0:
+        return r
+    n = tracks["hitsNum"].astype(np.int64)
+    hits = tracks["hits"].astype(np.int64)
+    mask = np.arange(hits.shape[1])[None, :] < n[:, None]
+    keys = (hit_id[np.where(mask, hits, 0)] >> np.uint32(8)).astype(np.int64)
+    keys = np.where(mask, keys, -1)
+    # majority key per track: compare every slot against every slot
+    eq = (keys[:, :, None] == keys[:, None, :]) & mask[:, None, :]
+    cnt = eq.sum(axis=2)
+    best = np.argmax(np.where(mask, cnt, -1), axis=1)
+    top_key = keys[np.arange(T), best]
+    top_cnt = cnt[np.arange(T), best]
+    matched = (top_key < NOISE_KEY_BASE) & (top_cnt >= PURITY * n)
+    r.ghosts = int((~matched).sum())
+    mk = top_key[matched]
+    if len(mk):
+        uniq, mult = np.unique(mk, return_counts=True)
+        r.clones = int((mult - 1).sum())
+        idx = uniq - 1
+        ok = (idx >= 0) & (idx < len(recon))
+        idx = idx[ok]
+        good = recon[idx]
+        r.matched = int(good.sum())
+        r.matched_low = int((good & low[idx]).sum())
+        r.matched_high = int((good & ~low[idx]).sum())
+    return r
+
+
+def rates_fast(all_tracks, blobs: Sequence[bytes], truths: Sequence[Truth]) -> Rates:
+    total = Rates()
+    for t, b, tr in zip(all_tracks, blobs, truths):
+        S, H = np.frombuffer(b[:8], "<i4")
+        ids = np.frombuffer(b, "<u4", int(H), 8 + 12 * int(S))
+        total.add(event_rates_fast(t, ids, tr))
+    return total

@@ -63,6 +63,7 @@ typedef enum velo_status {
 #define VELO_EVENT_MAX_TRACKS 0x4u      /* more than MAX_TRACKS tracks (Kernel.cl:336,810) */
 #define VELO_EVENT_INVALID 0x8u         /* blob failed validation; no tracks */
 #define VELO_EVENT_DEGENERATE 0x10u     /* an inf/NaN fit (two modules' hits at equal z) */
+#define VELO_EVENT_LEARNED_FALLBACK 0x20u  /* learned seeding kept too few doublets; rerun plain */
 
 typedef enum velo_launch_mode {
   VELO_LAUNCH_PER_EVENT = 0,   /* one CTA per event (the reference's one work-group per event) */
@@ -79,7 +80,9 @@ typedef struct velo_options {
   int32_t use_graph;          /* 1: capture the launch sequence in a CUDA graph and replay it */
   int32_t register_ctas;      /* 4 or 5: kernel build whose registers fit that many 256-thread
                                  CTAs per SM (fewer registers, more CTAs); 0 = 5 */
-  int32_t reserved[8];
+  int32_t learned;            /* 1: seeding prunes doublets with the MLP set by velo_set_mlp
+                                 (approximate; no counterpart in the reference) */
+  int32_t reserved[7];
 } velo_options;
 
 typedef struct velo_stats {
@@ -161,6 +164,47 @@ velo_status velo_time_runs(velo_ctx* ctx, const velo_options* opts, int32_t warm
  * `base`. */
 velo_status velo_autotune(velo_ctx* ctx, const velo_options* base, int32_t iters,
                           velo_options* best_out, float* best_ms_out);
+
+/*
+ * Learned doublet pruning (no counterpart in the reference).  A 10 -> 32 -> 32
+ * -> 2 ReLU MLP scores each (h0, h1) seed doublet before its h2 search: a
+ * keep logit, and the half-width (mm) of the x window around the predicted h2
+ * position.  Doublets whose logit is below keep_threshold are skipped; the
+ * others search h2 only within half-width + window_margin (never wider than
+ * the exact cut).  An event whose kept fraction of doublets falls below
+ * min_keep_rate is re-searched by the plain method and flagged
+ * VELO_EVENT_LEARNED_FALLBACK.  Parameters: W1[32][10] b1[32] W2[32][32]
+ * b2[32] W3[2][32] b3[2], FP32.
+ */
+#define VELO_MLP_INPUTS 10
+#define VELO_MLP_HIDDEN 32
+#define VELO_MLP_OUTPUTS 2
+#define VELO_MLP_PARAMS 1474
+velo_status velo_set_mlp(velo_ctx* ctx, const float* weights, float keep_threshold, float window_margin,
+                         float min_keep_rate);
+
+/* Training data: runs the plain search on the staged events and records,
+ * for one in `keep_one_in` of the doublets that reach the h2 search (hashed
+ * on event, h0, h1), the VELO_MLP_INPUTS features the learned seeding sees
+ * and {event, h0, h1}.  Up to `capacity` records; count_out gets how many
+ * were produced (possibly more than capacity).  velo_fetch then returns the
+ * tracks, from which labels follow. */
+velo_status velo_dump_doublets(velo_ctx* ctx, const velo_options* opts, uint32_t keep_one_in,
+                               float* features_out, uint32_t* ids_out, uint64_t capacity,
+                               uint64_t* count_out);
+
+/* MLP training and evaluation on the current CUDA device (hand-written
+ * kernels; inputs are host arrays, n samples of VELO_MLP_INPUTS features,
+ * labels in {0, 1}, width targets in mm).  velo_mlp_train runs `steps` Adam
+ * steps on batches of `batch` samples drawn without replacement per epoch and
+ * updates weights_inout; loss_per_step (optional) receives each step's mean
+ * loss.  velo_mlp_grad gives the mean-loss gradient at `weights`;
+ * velo_mlp_forward the n x 2 outputs. */
+velo_status velo_mlp_train(const float* x, const float* label, const float* target, int64_t n, int32_t steps,
+                           int32_t batch, float lr, uint64_t seed, float* weights_inout, float* loss_per_step);
+velo_status velo_mlp_grad(const float* weights, const float* x, const float* label, const float* target,
+                          int64_t n, float* grad_out, float* loss_out);
+velo_status velo_mlp_forward(const float* weights, const float* x, int64_t n, float* out);
 
 /* Pinned host memory (cudaHostAlloc), for callers without a CUDA runtime. */
 velo_status velo_host_alloc(velo_ctx* ctx, uint64_t bytes, void** ptr);

@@ -54,3 +54,13 @@ def test_compare_events_order_independent():
     assert validation.compare_events([a], [b], [blob]) == []
     c = np.concatenate([_track([0, 1, 2]), _track([3, 4])])
     assert validation.compare_events([a], [c], [blob]) == [0]
+
+
+def test_fast_rates_equal_reference_rates():
+    from oracle import oracle
+    blobs, truths = generator.generate(range(40))
+    sb = [oracle.sort_by_x(b) for b in blobs]
+    tracks, _ = oracle.search(sb, 4)
+    slow = validation.rates(tracks, sb, truths)
+    fast = validation.rates_fast(tracks, sb, truths)
+    assert slow == fast
