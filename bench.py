@@ -73,6 +73,7 @@ def parse_args():
     ap.add_argument("--e2e-chunk", type=int, default=16000, help="events per end-to-end call")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-pruning leg")
     ap.add_argument("--ref-emulator", action="store_true",
                     help="reference arm: time the reference kernel under the work-group emulator "
                          "(oracle/_ref, only where it was built) instead of the oracle restatement")
@@ -257,6 +258,67 @@ def reference_arm(args, ranks: Ranks):
     }
 
 
+PROFILES = {"scale": "search_kernel_scale7k_full.md"}
+
+
+def profiled_traffic(config: str, n_events: int):
+    """DRAM bytes of one launch: the ncu capture's bytes per event x events.
+
+    The capture ran on 7,000 events of the same workload (a full 10,000-event
+    capture would exceed the size a 45-pass ncu replay can take in minutes);
+    DRAM traffic grows in proportion to the events processed, so it scales.
+    """
+    name = PROFILES.get(config)
+    if not name:
+        return None, None
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_event:"):
+                per = int(ln.split(":")[1])
+                return per * n_events, f"profiles/{name}: {per} B/event x {n_events} events"
+    except OSError:
+        pass
+    return None, None
+
+
+LEARNED_WEIGHTS = os.path.join(ROOT, "cl_forward_gb300", "weights", "doublet_mlp.npz")
+
+
+def learned_leg(ctx, hbuf, offs, sizes, blobs, truths, opts, tracks, counts, first, plain_ms, args):
+    """The learned-pruned search of the same staged events next to the plain one."""
+    import numpy as np
+    from cl_forward_gb300 import native
+    from cl_forward_gb300.validation import rates_fast
+    wz = np.load(LEARNED_WEIGHTS)
+    ctx.set_mlp(wz["weights"], float(wz["keep_threshold"]), float(wz["window_margin"]),
+                float(wz["min_keep_rate"]))
+    o = native.Options.from_buffer_copy(opts)
+    o.learned = 1
+    o.use_graph = 0
+    ctx.stage(hbuf, offs, sizes)
+    for _ in range(args.warmup):
+        ctx.run(o)
+    ctx.synchronize()
+    steps_ms = [ctx.time_runs(o, warmup=0, iters=1, flush_l2=True) for _ in range(args.steps)]
+    n = len(blobs)
+    cap = len(tracks)
+    lt, lc, lf, ls = ctx.fetch(n, cap)
+    per_l = [lt[int(lf[e]):int(lf[e]) + int(lc[e])] for e in range(n)]
+    per_p = [tracks[int(first[e]):int(first[e]) + int(counts[e])] for e in range(n)]
+    rp = rates_fast(per_p, blobs, truths)
+    rl = rates_fast(per_l, blobs, truths)
+    ms = statistics.fmean(steps_ms)
+    return {"value": n / (ms / 1e3), "unit": "events/s", "ms_per_step": ms, "speedup_vs_plain": plain_ms / ms,
+            "efficiency_plain": rp.efficiency, "efficiency_learned": rl.efficiency,
+            "efficiency_loss": rp.efficiency - rl.efficiency, "ghost_rate_plain": rp.ghost_rate,
+            "ghost_rate_learned": rl.ghost_rate, "ghost_increase": rl.ghost_rate - rp.ghost_rate,
+            "clone_change": rl.clone_rate - rp.clone_rate,
+            "fallback_fraction": float(np.mean((ls & native.EVENT_LEARNED_FALLBACK) != 0)),
+            "weights": os.path.relpath(LEARNED_WEIGHTS, ROOT), "weights_sha256": str(wz["sha256"]),
+            "note": "same events, same launch shape; the network is trained on other seeds (100000-149999)"}
+
+
 # ---------------------------------------------------------------- GPU arm --
 def gpu_arm(args, ranks: Ranks):
     import numpy as np
@@ -354,6 +416,7 @@ def gpu_arm(args, ranks: Ranks):
     else:
         peak, peak_src = 6800.0, "fallback"
     achieved = alg_bytes / (ms / 1e3) / 1e9
+    traffic, traffic_src = profiled_traffic(args.config, n)
     _, _, _, _, desc = CONFIGS[args.config]
     line = {
         "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus, "steps": args.steps,
@@ -373,14 +436,17 @@ def gpu_arm(args, ranks: Ranks):
         "e2e": {"value": ranks.sum(n) / e2e_max, "unit": "events/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "peak_source": peak_src,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "algorithmic_bytes": alg_bytes, "peak_source": peak_src,
                      "note": "algorithmic bytes = input blobs + 4 B count + 100 B per track"},
         "clocks": clk.summary(),
         "gpu_launches": launches,
         "status_flags": {"ring_overflow": int(np.sum(status & 1 != 0)),
                          "track_overflow": int(np.sum(status & 2 != 0))},
     }
+    if not args.no_learned and os.path.exists(LEARNED_WEIGHTS):
+        line["learned"] = learned_leg(ctx, hbuf, offs, sizes, blobs, truths, opts, tracks, counts, first, ms,
+                                      args)
     if ranks.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(blobs, args.cpu_seconds)
     ctx.host_free(hbuf)

@@ -37,7 +37,7 @@ struct velo_ctx {
 
   DevBuf d_input, d_ev_offset, d_ev_hits, d_ev_maxmod, d_ev_valid, d_hit_base, d_arena_off, d_order;
   DevBuf d_tracklets, d_weak, d_tracks, d_out_tracks, d_out_counts, d_out_first, d_out_status;
-  DevBuf d_counters, d_garena, d_flush;
+  DevBuf d_counters, d_garena, d_flush, d_fits;
 
   // staged batch
   bool staged = false;
@@ -286,7 +286,7 @@ void velo_destroy(velo_ctx* c) {
                     &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_weak,
                     &c->d_tracks, &c->d_out_tracks, &c->d_out_counts, &c->d_out_first,
                     &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush, &c->d_mlp,
-                    &c->d_dump_features, &c->d_dump_ids};
+                    &c->d_dump_features, &c->d_dump_ids, &c->d_fits};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -793,6 +793,55 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
           }
         }
   if (best_ms_out) *best_ms_out = best;
+  return VELO_OK;
+}
+
+velo_status velo_sort_staged(velo_ctx* c) {
+  if (!c) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->staged) return VELO_ERR_NOT_STAGED;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  const int e = velo::launch_sort_modules(P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset),
+                                          P<uint32_t>(c->d_ev_valid), c->n, c->stream);
+  if (e != 0) return cuda_fail(c, (cudaError_t)e, "sort kernel launch");
+  return VELO_OK;
+}
+
+velo_status velo_fit_tracks(velo_ctx* c, velo_track_fit* fits_out, uint64_t capacity) {
+  if (!c || (!fits_out && capacity)) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->ran) return VELO_ERR_NOT_STAGED;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  velo_status st = ensure(c, c->d_fits, sizeof(velo_track_fit) * (c->rows ? c->rows : 1), "fits");
+  if (st != VELO_OK) return st;
+  unsigned long long total = 0;
+  VELO_CUDA(c, cudaMemcpyAsync(&total, c->d_counters.p, 8, cudaMemcpyDeviceToHost, c->stream));
+  const int e = velo::launch_fit_tracks(P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset),
+                                        P<uint32_t>(c->d_ev_valid), P<velo_track>(c->d_out_tracks),
+                                        P<uint32_t>(c->d_out_counts), P<uint64_t>(c->d_out_first), c->n,
+                                        P<velo_track_fit>(c->d_fits), c->stream);
+  if (e != 0) return cuda_fail(c, (cudaError_t)e, "fit kernel launch");
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (total > capacity) {
+    c->err = "fit buffer too small";
+    return VELO_ERR_CAPACITY;
+  }
+  if (total)
+    VELO_CUDA(c, cudaMemcpyAsync(fits_out, c->d_fits.p, sizeof(velo_track_fit) * total, cudaMemcpyDeviceToHost,
+                                 c->stream));
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  return VELO_OK;
+}
+
+velo_status velo_fetch_staged(velo_ctx* c, uint8_t* buf, uint64_t size) {
+  if (!c || (!buf && size)) return VELO_ERR_INVALID_ARGUMENT;
+  if (!c->staged) return VELO_ERR_NOT_STAGED;
+  if (size < c->input_bytes) {
+    c->err = "buffer smaller than the staged events";
+    return VELO_ERR_CAPACITY;
+  }
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  if (c->input_bytes)
+    VELO_CUDA(c, cudaMemcpyAsync(buf, c->d_input.p, c->input_bytes, cudaMemcpyDeviceToHost, c->stream));
+  VELO_CUDA(c, cudaStreamSynchronize(c->stream));
   return VELO_OK;
 }
 

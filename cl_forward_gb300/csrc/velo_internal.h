@@ -122,6 +122,12 @@ int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_byte
 int configure_search_kernel(uint32_t smem_bytes);
 // Maximum resident CTAs per SM for a block size, shared-memory size and build.
 int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, int* ctas_per_sm);
+// Straight-line fits of the compacted output tracks (velo_fit.cu).
+int launch_fit_tracks(const uint8_t* input, const uint64_t* ev_offset, const uint32_t* ev_valid,
+                      const velo_track* tracks, const uint32_t* counts, const uint64_t* first, int n_events,
+                      velo_track_fit* fits, void* stream);
+// Sorts each module's hits by x in place on staged events (velo_sort.cu).
+int launch_sort_modules(uint8_t* input, const uint64_t* offsets, const uint32_t* valid, int n_events, void* stream);
 // kernel modes (velo_kernels.cu): plain, plain + training-data dump, learned
 constexpr int kModePlain = 0, kModeDump = 1, kModeLearned = 2;
 

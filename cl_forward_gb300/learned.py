@@ -115,19 +115,23 @@ def build_dataset(ctx: native.Context, blobs: Sequence[bytes], keep_one_in: int 
         if len(rows) == 0 or counts[e] == 0:
             continue
         t = tracks[int(first[e]):int(first[e]) + int(counts[e])]
-        seed = {int(h[0]): (int(h[1]), int(h[2])) for h in t["hits"][:, :3]}
+        seeds = t["hits"][:, :3].astype(np.int64)
+        seed_key = (seeds[:, 0] << 32) | seeds[:, 1]       # h0 seeds at most once: keys are unique
+        row_key = (ids[rows, 1].astype(np.int64) << 32) | ids[rows, 2].astype(np.int64)
+        srt = np.argsort(seed_key)
+        pos = np.searchsorted(seed_key[srt], row_key)
+        pos = np.minimum(pos, len(srt) - 1)
+        hit = seed_key[srt][pos] == row_key
+        if not hit.any():
+            continue
+        r = rows[hit]
+        h0, h1, h2 = (seeds[srt][pos[hit], k] for k in range(3))
         ev = unpack_event(blobs[e])
-        h0s, h1s = ids[rows, 1], ids[rows, 2]
-        for r, h0, h1 in zip(rows, h0s, h1s):
-            s = seed.get(int(h0))
-            if s is None or s[0] != int(h1):
-                continue
-            h2 = s[1]
-            x0, z0 = float(ev.x[h0]), float(ev.z[h0])
-            x1, z1 = float(ev.x[h1]), float(ev.z[h1])
-            xp = x0 + (x1 - x0) * (float(ev.z[h2]) - z0) / (z1 - z0)
-            label[r] = 1.0
-            target[r] = abs(xp - float(ev.x[h2]))
+        x0, z0 = ev.x[h0].astype(np.float64), ev.z[h0].astype(np.float64)
+        x1, z1 = ev.x[h1].astype(np.float64), ev.z[h1].astype(np.float64)
+        xp = x0 + (x1 - x0) * (ev.z[h2].astype(np.float64) - z0) / (z1 - z0)
+        label[r] = 1.0
+        target[r] = np.abs(xp - ev.x[h2].astype(np.float64))
     return Dataset(feats, label, target, len(blobs))
 
 

@@ -45,8 +45,11 @@ EXPORTED = [
     "velo_search_packed", "velo_stage", "velo_run", "velo_fetch", "velo_synchronize",
     "velo_get_stats", "velo_time_runs", "velo_host_alloc", "velo_host_free", "velo_device_sm_count",
     "velo_search_device_static", "velo_autotune", "velo_set_mlp", "velo_dump_doublets",
-    "velo_mlp_train", "velo_mlp_grad", "velo_mlp_forward",
+    "velo_mlp_train", "velo_mlp_grad", "velo_mlp_forward", "velo_sort_staged", "velo_fetch_staged",
+    "velo_fit_tracks",
 ]
+
+FIT_DTYPE = np.dtype([("x0", "<f4"), ("tx", "<f4"), ("y0", "<f4"), ("ty", "<f4"), ("chi2_ndf", "<f4")])
 
 MLP_INPUTS = 10
 MLP_HIDDEN = 32
@@ -132,6 +135,9 @@ def load() -> ctypes.CDLL:
     l.velo_mlp_train.argtypes = [vp, vp, vp, ctypes.c_int64, i32, i32, f32, u64, vp, vp]
     l.velo_mlp_grad.argtypes = [vp, vp, vp, vp, ctypes.c_int64, vp, ctypes.POINTER(f32)]
     l.velo_mlp_forward.argtypes = [vp, vp, ctypes.c_int64, vp]
+    l.velo_sort_staged.argtypes = [vp]
+    l.velo_fetch_staged.argtypes = [vp, vp, u64]
+    l.velo_fit_tracks.argtypes = [vp, vp, u64]
     _lib = l
     return l
 
@@ -282,6 +288,35 @@ class Context:
                                                  capacity, ctypes.byref(count)), "velo_dump_doublets")
         k = min(int(count.value), capacity)
         return feats[:k], ids[:k], int(count.value)
+
+    def fit_tracks(self, capacity: int) -> np.ndarray:
+        """Straight-line fits of the last run's tracks, in fetch order."""
+        fits = np.zeros(max(capacity, 1), FIT_DTYPE)
+        self._check(self._lib.velo_fit_tracks(self._h, _p(fits), capacity), "velo_fit_tracks")
+        return fits
+
+    def sort_staged(self):
+        """The reference's per-module x-sort, on the device, of the staged events."""
+        self._check(self._lib.velo_sort_staged(self._h), "velo_sort_staged")
+
+    def fetch_staged(self, nbytes: int) -> np.ndarray:
+        buf = np.zeros(max(nbytes, 1), np.uint8)
+        self._check(self._lib.velo_fetch_staged(self._h, _p(buf), nbytes), "velo_fetch_staged")
+        return buf[:nbytes]
+
+    def search_unsorted(self, blobs: Sequence[bytes], options: Optional[Options] = None):
+        """Sort on the device, then search: (tracks per event, status, x-sorted blobs)."""
+        from .events import pack_events
+        buf, offs, sizes = pack_events(blobs)
+        self.stage(buf, offs, sizes)
+        self.sort_staged()
+        self.run(options or default_options())
+        cap = int(sum(max(int(np.frombuffer(b[4:8], "<i4")[0]), 1) if len(b) >= 8 else 1 for b in blobs))
+        tracks, counts, first, status = self.fetch(len(blobs), cap)
+        staged = self.fetch_staged(int(offs[-1] + sizes[-1]) if len(blobs) else 0)
+        sorted_blobs = [staged[int(o):int(o) + int(n)].tobytes() for o, n in zip(offs, sizes)]
+        per = [tracks[int(first[e]):int(first[e]) + int(counts[e])] for e in range(len(blobs))]
+        return per, status, sorted_blobs
 
     def stats(self) -> Stats:
         s = Stats()

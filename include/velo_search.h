@@ -43,6 +43,14 @@ typedef struct velo_track {
   uint32_t hits[VELO_MAX_TRACK_SIZE];
 } velo_track;
 
+/* Straight-line fit of one track: x = x0 + tx z, y = y0 + ty z (mm, z in mm),
+ * least squares with equal hit weights; chi2_ndf uses the pixel weight
+ * PARAM_W = 3966.94 / mm^2 (KernelDefinitions.h:25).  No counterpart in the
+ * search kernel; it is the stage that follows it. */
+typedef struct velo_track_fit {
+  float x0, tx, y0, ty, chi2_ndf;
+} velo_track_fit;
+
 typedef enum velo_status {
   VELO_OK = 0,
   VELO_ERR_INVALID_ARGUMENT = -1,
@@ -146,6 +154,20 @@ velo_status velo_run(velo_ctx* ctx, const velo_options* opts);
 velo_status velo_fetch(velo_ctx* ctx, velo_track* tracks_out, uint64_t track_capacity,
                        uint32_t* counts_out, uint64_t* first_out, uint32_t* event_status_out);
 velo_status velo_synchronize(velo_ctx* ctx);
+
+/* preorder_by_x (Tools.cpp:46-66) on the device: sorts each module's hits of
+ * the staged events by x, in place, with the same permutation as the
+ * reference (equal x included).  Sort once per staged batch, before
+ * velo_run; output hit indices then refer to the sorted order, which
+ * velo_fetch_staged returns (the staged bytes, in the layout given to
+ * velo_stage: event e at buf + offsets[e] - min(offsets)). */
+velo_status velo_sort_staged(velo_ctx* ctx);
+
+/* Fits every track of the last run (velo_run / velo_search) on the device and
+ * copies the fits to fits_out, in the order of the tracks velo_fetch returns
+ * (fits_out[first[e] + i] belongs to tracks_out[first[e] + i]). */
+velo_status velo_fit_tracks(velo_ctx* ctx, velo_track_fit* fits_out, uint64_t capacity);
+velo_status velo_fetch_staged(velo_ctx* ctx, uint8_t* buf, uint64_t size);
 velo_status velo_get_stats(const velo_ctx* ctx, velo_stats* stats);
 
 /* `iters` back-to-back velo_run calls on the staged events, timed with CUDA

@@ -200,3 +200,49 @@ def test_split_stage_run_fetch(gpu_ctx, oracle_lib):
     s = gpu_ctx.stats()
     assert s.launches == 1 and s.n_events == len(blobs) and s.total_tracks == counts.sum()
     assert gpu_ctx.time_runs(native.default_options(), warmup=1, iters=2, flush_l2=True) > 0
+
+
+def test_device_sort_matches_reference_sort(gpu_ctx, oracle_lib, golden):
+    """velo_sort_staged: the reference's preorder_by_x permutation, ties included."""
+    from cl_forward_gb300 import fuzz, generator
+    for name in ("velo", "fuzz", "edge"):
+        raw = golden[name]["input"]
+        _, _, sorted_blobs = gpu_ctx.search_unsorted(raw)
+        assert sorted_blobs == golden[name]["sorted"], name
+    raw = generator.generate(range(2000, 2030))[0] + [fuzz.fuzz_event(s, grid=2.0) for s in range(30)]
+    got, status, sorted_blobs = gpu_ctx.search_unsorted(raw)
+    assert sorted_blobs == [oracle_lib.sort_by_x(b) for b in raw]
+    want, _ = oracle_lib.search(sorted_blobs, 4)
+    for e in range(len(raw)):
+        if not (status[e] & OVERFLOW_BITS):
+            assert index_lists(got[e]) == index_lists(want[e])
+
+
+def test_track_fits_match_least_squares(gpu_ctx, oracle_lib):
+    """velo_fit_tracks against a float64 least-squares fit (tolerance 1e-4 mm, 1e-6 in slope)."""
+    from cl_forward_gb300 import events, generator
+    blobs = [oracle_lib.sort_by_x(b) for b in generator.generate(range(3000, 3020))[0]]
+    buf, offs, sizes = events.pack_events(blobs)
+    gpu_ctx.stage(buf, offs, sizes)
+    gpu_ctx.run()
+    cap = int(sum(max(int(np.frombuffer(b[4:8], "<i4")[0]), 1) for b in blobs))
+    tracks, counts, first, _ = gpu_ctx.fetch(len(blobs), cap)
+    fits = gpu_ctx.fit_tracks(cap)
+    checked = 0
+    for e, blob in enumerate(blobs):
+        ev = events.unpack_event(blob)
+        for i in range(int(counts[e])):
+            t = tracks[int(first[e]) + i]
+            h = t["hits"][:int(t["hitsNum"])]
+            z = ev.z[h].astype(np.float64)
+            A = np.stack([np.ones_like(z), z], 1)
+            (x0, tx), *_ = np.linalg.lstsq(A, ev.x[h].astype(np.float64), rcond=None)
+            (y0, ty), *_ = np.linalg.lstsq(A, ev.y[h].astype(np.float64), rcond=None)
+            f = fits[int(first[e]) + i]
+            assert abs(f["tx"] - tx) < 1e-6 + 1e-5 * abs(tx) and abs(f["ty"] - ty) < 1e-6 + 1e-5 * abs(ty)
+            assert abs(f["x0"] - x0) < 1e-4 + 1e-5 * abs(x0) and abs(f["y0"] - y0) < 1e-4 + 1e-5 * abs(y0)
+            r = np.concatenate([ev.x[h] - (x0 + tx * z), ev.y[h] - (y0 + ty * z)])
+            chi2 = 3966.94 * float(r @ r) / (2 * len(h) - 4)
+            assert abs(f["chi2_ndf"] - chi2) <= 1e-3 * max(chi2, 1e-3) + 1e-4
+            checked += 1
+    assert checked > 1000
