@@ -71,6 +71,8 @@ def parse_args():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the library's default launch configuration instead of the autotuned one")
     ap.add_argument("--e2e-chunk", type=int, default=16000, help="events per end-to-end call")
+    ap.add_argument("--e2e-pipeline", type=int, default=2500,
+                    help="events per overlapped part inside an end-to-end call (0: one part)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-pruning leg")
@@ -202,8 +204,12 @@ class Clocks:
 
 
 # ------------------------------------------------------------- baselines --
-def cpu_baseline(blobs, seconds: float):
-    """Oracle restatement over all host cores, repeated passes until `seconds`."""
+def cpu_baseline(blobs, seconds: float, raw=None):
+    """Oracle restatement over all host cores, repeated passes until `seconds`.
+
+    Also: the other Y-lane counts the reference sweeps (KernelInvoker.cpp:149-153)
+    and the host x-sort, each on a 2,000-event sample, and the oracle's count
+    of candidate evaluations per event (the reference algorithm's work)."""
     from oracle import oracle
     n = len(blobs)
     passes, elapsed = 0, 0.0
@@ -211,9 +217,29 @@ def cpu_baseline(blobs, seconds: float):
         elapsed += oracle.time_search(blobs, 4, 0)
         passes += 1
     cores = os.cpu_count() or 1
-    return {"value": n * passes / elapsed, "unit": "events/s", "cores": cores, "kind": "port",
+    sample = blobs[:2000]
+    per_y = {}
+    for y in (1, 2, 3, 4):
+        per_y[str(y)] = len(sample) / min(oracle.time_search(sample, y, 0) for _ in range(2))
+    sort_s = None
+    if raw is not None:
+        t0 = time.perf_counter()
+        for b in raw[:len(sample)]:
+            oracle.sort_by_x(b)
+        sort_s = (time.perf_counter() - t0) / len(sample)
+    _, _, cnt = oracle.search(blobs[:500], 4, 0, counters=True)
+    m = max(min(500, n), 1)
+    work = {"window_evals": cnt.window_evals / m, "forward_fits": cnt.forward_fits / m,
+            "seed_fits": cnt.seed_fits / m, "seed_scatters": cnt.seed_scatters / m,
+            "sample_events": m}
+    ev_s = n * passes / elapsed
+    return {"value": ev_s, "unit": "events/s", "cores": cores, "kind": "port",
             "sample": f"{passes} pass(es) over the same {n} x-sorted events, Y=4, {cores} threads, "
-                      f"{elapsed:.1f} s, search only (sort excluded, as on the GPU)"}
+                      f"{elapsed:.1f} s, search only (sort excluded, as on the GPU)",
+            "events_per_s_by_y": per_y, "best_y": max(per_y, key=per_y.get),
+            "host_sort_us_per_event_one_thread": None if sort_s is None else 1e6 * sort_s,
+            "events_per_s_with_sort": None if sort_s is None else 1.0 / (1.0 / ev_s + sort_s / cores),
+            "work_per_event": work}
 
 
 def reference_arm(args, ranks: Ranks):
@@ -291,8 +317,9 @@ def learned_leg(ctx, hbuf, offs, sizes, blobs, truths, opts, tracks, counts, fir
     from cl_forward_gb300 import native
     from cl_forward_gb300.validation import rates_fast
     wz = np.load(LEARNED_WEIGHTS)
+    max_hits = int(wz["max_event_hits"]) if "max_event_hits" in wz.files else 0
     ctx.set_mlp(wz["weights"], float(wz["keep_threshold"]), float(wz["window_margin"]),
-                float(wz["min_keep_rate"]))
+                float(wz["min_keep_rate"]), max_hits)
     o = native.Options.from_buffer_copy(opts)
     o.learned = 1
     o.use_graph = 0
@@ -316,6 +343,7 @@ def learned_leg(ctx, hbuf, offs, sizes, blobs, truths, opts, tracks, counts, fir
             "clone_change": rl.clone_rate - rp.clone_rate,
             "fallback_fraction": float(np.mean((ls & native.EVENT_LEARNED_FALLBACK) != 0)),
             "weights": os.path.relpath(LEARNED_WEIGHTS, ROOT), "weights_sha256": str(wz["sha256"]),
+            "max_event_hits": max_hits,
             "note": "same events, same launch shape; the network is trained on other seeds (100000-149999)"}
 
 
@@ -392,9 +420,12 @@ def gpu_arm(args, ranks: Ranks):
     h_first = np.zeros(n, np.uint64)
     h_status = np.zeros(n, np.uint32)
 
+    e2e_opts = native.Options.from_buffer_copy(opts)
+    e2e_opts.pipeline_events = args.e2e_pipeline
+
     def e2e_pass():
         for a, b in bounds:
-            ctx.search_packed_into(hbuf, offs[a:b], sizes[a:b], opts, h_tracks, h_counts[a:b], h_first[a:b],
+            ctx.search_packed_into(hbuf, offs[a:b], sizes[a:b], e2e_opts, h_tracks, h_counts[a:b], h_first[a:b],
                                    h_status[a:b])
 
     for _ in range(args.warmup):
@@ -429,7 +460,7 @@ def gpu_arm(args, ranks: Ranks):
                    "ms_per_step_samples": [round(x, 4) for x in steps_ms],
                    "register_ctas": opts.register_ctas, "cuda_graph": bool(opts.use_graph),
                    "smem_hits_option": opts.smem_hits, "autotuned": tuned,
-                   "e2e_chunk_events": chunk,
+                   "e2e_chunk_events": chunk, "e2e_pipeline_events": args.e2e_pipeline,
                    "l2": "flushed between timed steps (2 x L2 memset); input also larger than L2",
                    "parallelism": f"weak scaling over {args.gpus} GPU(s), event blocks per rank"},
         "impl": "gb300",
@@ -448,7 +479,13 @@ def gpu_arm(args, ranks: Ranks):
         line["learned"] = learned_leg(ctx, hbuf, offs, sizes, blobs, truths, opts, tracks, counts, first, ms,
                                       args)
     if ranks.rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(blobs, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(blobs, args.cpu_seconds, raw)
+        wk = line["cpu_baseline"]["work_per_event"]
+        # candidate evaluations of the reference algorithm per event x events/s of the
+        # GPU (the GPU skips most of them: narrowed windows)
+        line["work"] = {"reference_evals_per_event": wk["window_evals"] + wk["forward_fits"] + wk["seed_fits"],
+                        "reference_evals_per_s": (wk["window_evals"] + wk["forward_fits"] + wk["seed_fits"])
+                        * value, "counted_by": "oracle restatement on 500 of the events"}
     ctx.host_free(hbuf)
     ctx.host_free(h_tracks.view(np.uint8))
     ctx.close()

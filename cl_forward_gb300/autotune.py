@@ -20,9 +20,12 @@ CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "auto
 FIELDS = ("threads_per_event", "launch_mode", "smem_hits", "narrow_windows", "register_ctas")
 
 
+SPACE = 2   # bumped when velo_autotune's candidate set changes: older entries are ignored
+
+
 def shape_key(sm_count: int, n_events: int, mean_hits: float, y_lanes: int) -> str:
     b = lambda v: 2 ** int(round(math.log2(max(v, 1))))
-    return f"sm{sm_count}-ev{b(n_events)}-hits{b(mean_hits)}-y{y_lanes}"
+    return f"sm{sm_count}-ev{b(n_events)}-hits{b(mean_hits)}-y{y_lanes}-s{SPACE}"
 
 
 def _load(path: str) -> dict:

@@ -70,6 +70,14 @@ struct velo_ctx {
   DevBuf d_mlp;
   bool mlp_set = false;
   float keep_threshold = 0.f, window_margin = 0.f, min_keep_rate = 0.f;
+  uint32_t learned_max_hits = 0;   // 0: no limit
+  std::vector<float> h_mlp;        // host copy, handed on to the pipeline contexts
+  uint64_t mlp_version = 0;
+
+  // pipelined searches (velo_options.pipeline_events): two child contexts,
+  // each with its own stream and buffers, that alternate over the parts
+  velo_ctx* pipe[2] = {nullptr, nullptr};
+  uint64_t pipe_mlp_version[2] = {0, 0};
   // training-data dump of the next launch (velo_dump_doublets)
   DevBuf d_dump_features, d_dump_ids;
   uint64_t dump_capacity = 0;
@@ -280,6 +288,8 @@ velo_status velo_create(velo_ctx** out, int32_t device) {
 
 void velo_destroy(velo_ctx* c) {
   if (!c) return;
+  velo_destroy(c->pipe[0]);
+  velo_destroy(c->pipe[1]);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->d_input, &c->d_ev_offset, &c->d_ev_hits, &c->d_ev_maxmod, &c->d_ev_valid,
@@ -463,6 +473,10 @@ velo_status check_options(velo_ctx* c, const velo_options* opts, velo_options* o
     return VELO_ERR_INVALID_ARGUMENT;
   }
   o->threads_per_event = (int32_t)resolve_threads(o->threads_per_event);
+  if (o->pipeline_events < 0) {
+    c->err = "pipeline_events must be >= 0";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
   if (o->register_ctas == 0) o->register_ctas = 5;
   if (o->register_ctas != 4 && o->register_ctas != 5) {
     c->err = "register_ctas must be 4 or 5";
@@ -542,6 +556,7 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
     p.keep_threshold = c->keep_threshold;
     p.window_margin = c->window_margin;
     p.min_keep_rate = c->min_keep_rate;
+    p.learned_max_hits = c->learned_max_hits;
   }
   if (c->dump_armed) {
     p.dump_features = P<float>(c->d_dump_features);
@@ -662,10 +677,116 @@ velo_status velo_get_stats(const velo_ctx* c, velo_stats* s) {
   return VELO_OK;
 }
 
+namespace {
+
+// A batch cut into parts of o.pipeline_events events that alternate between
+// two child contexts: while part k is searched on one stream, part k+1's
+// events go up and part k-1's tracks come down on the other.  Each part's
+// tracks land after the previous part's in tracks_out; first[] is rebased.
+velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
+                             int32_t n, const velo_options& o, velo_track* tracks_out, uint64_t capacity,
+                             uint32_t* counts, uint64_t* first, uint32_t* status) {
+  velo_options po = o;
+  po.pipeline_events = 0;
+  po.use_graph = 0;   // parts differ in size; a graph per part would be captured once and replayed once
+  for (int k = 0; k < 2; ++k) {
+    if (!c->pipe[k]) {
+      velo_status st = velo_create(&c->pipe[k], c->device);
+      if (st != VELO_OK) {
+        c->err = "pipeline context: " + std::string(velo_status_string(st));
+        return st;
+      }
+    }
+    if (o.learned && c->pipe_mlp_version[k] != c->mlp_version) {
+      velo_status st = velo_set_mlp(c->pipe[k], c->h_mlp.data(), c->keep_threshold, c->window_margin,
+                                    c->min_keep_rate, c->learned_max_hits);
+      if (st != VELO_OK) {
+        c->err = c->pipe[k]->err;
+        return st;
+      }
+      c->pipe_mlp_version[k] = c->mlp_version;
+    }
+  }
+  // the parent holds no batch from here on
+  c->staged = false;
+  c->ran = false;
+  c->generation++;
+  const int32_t part = o.pipeline_events;
+  const int32_t n_parts = (n + part - 1) / part;
+  uint64_t base = 0, hits = 0, in_bytes = 0;
+  float kernel_ms = 0.f;
+  int32_t bad_event = -1;
+  velo_status first_error = VELO_OK;
+  auto finish = [&](int32_t k) -> velo_status {
+    velo_ctx* ch = c->pipe[k & 1];
+    const int32_t a = k * part, b = std::min(n, a + part);
+    const bool want_tracks = tracks_out != nullptr || capacity != 0;
+    velo_status st = velo_fetch(ch, want_tracks ? tracks_out + base : nullptr,
+                                want_tracks ? (capacity > base ? capacity - base : 0) : 0,
+                                counts ? counts + a : nullptr, first ? first + a : nullptr,
+                                status ? status + a : nullptr);
+    if (st != VELO_OK) {
+      c->err = ch->err;
+      return st;
+    }
+    if (first)
+      for (int32_t e = a; e < b; ++e) first[e] += base;
+    for (int32_t e = a; e < b && bad_event < 0; ++e)
+      if (ch->h_status[e - a] & VELO_EVENT_INVALID) bad_event = e;
+    base += ch->stats.total_tracks;
+    hits += ch->stats.total_hits;
+    in_bytes += ch->stats.input_bytes;
+    kernel_ms += ch->stats.kernel_ms;
+    return VELO_OK;
+  };
+  for (int32_t k = 0; k < n_parts; ++k) {
+    if (k >= 2 && first_error == VELO_OK) first_error = finish(k - 2);
+    if (first_error != VELO_OK) break;
+    velo_ctx* ch = c->pipe[k & 1];
+    const int32_t a = k * part, b = std::min(n, a + part);
+    velo_status st = velo_stage(ch, buf, offsets + a, sizes + a, b - a);
+    if (st == VELO_OK) st = velo_run(ch, &po);
+    if (st != VELO_OK) {
+      c->err = ch->err;
+      first_error = st;
+      break;
+    }
+  }
+  // drain: the last two parts (and, after an error, whatever is in flight)
+  for (int k = 0; k < 2; ++k) cudaStreamSynchronize(c->pipe[k]->stream);
+  if (first_error != VELO_OK) return first_error;
+  for (int32_t k = std::max(0, n_parts - 2); k < n_parts; ++k) {
+    velo_status st = finish(k);
+    if (st != VELO_OK) return st;
+  }
+  c->stats.n_events = (uint32_t)n;
+  c->stats.total_hits = hits;
+  c->stats.input_bytes = in_bytes;
+  c->stats.total_tracks = base;
+  c->stats.output_bytes = 4ull * n + sizeof(velo_track) * base;
+  c->stats.kernel_ms = kernel_ms;
+  c->stats.launches = (uint32_t)n_parts;
+  if (bad_event >= 0) {
+    c->err = "event " + std::to_string(bad_event) + " failed validation";
+    return VELO_ERR_INVALID_EVENT;
+  }
+  return VELO_OK;
+}
+
+}  // namespace
+
 velo_status velo_search_packed(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
                                const uint64_t* sizes, int32_t n, const velo_options* opts,
                                velo_track* tracks_out, uint64_t capacity, uint32_t* counts,
                                uint64_t* first, uint32_t* status) {
+  if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  if (opts && opts->pipeline_events > 0 && n > 2 * opts->pipeline_events) {
+    velo_options o;
+    velo_status st = check_options(c, opts, &o);
+    if (st != VELO_OK) return st;
+    VELO_CUDA(c, cudaSetDevice(c->device));
+    return search_pipelined(c, buf, offsets, sizes, n, o, tracks_out, capacity, counts, first, status);
+  }
   velo_status st = velo_stage(c, buf, offsets, sizes, n);
   if (st != VELO_OK) return st;
   if ((st = velo_run(c, opts)) != VELO_OK) return st;
@@ -765,8 +886,8 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
   // threads per event x shared-memory tile (hits staged per CTA; 0 = the
   // automatic budget) x register build x launch style; narrowing stays on
   // (it only removes work) and y_lanes is the caller's (it defines results)
-  static const int32_t kThreads[] = {128, 256};
-  static const int32_t kSmemHits[] = {0, 600, 900, 1200, 1600, 2400};
+  static const int32_t kThreads[] = {64, 128, 256, 512};
+  static const int32_t kSmemHits[] = {0, 300, 600, 900, 1200, 1600, 2400};
   static const int32_t kRegs[] = {4, 5};
   static const int32_t kModes[] = {VELO_LAUNCH_PER_EVENT, VELO_LAUNCH_PERSISTENT};
   float best = 0.f;
@@ -775,6 +896,7 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
     for (int32_t regs : kRegs)
       for (int32_t threads : kThreads)
         for (int32_t hits : kSmemHits) {
+          if (threads > 256 && regs != 5) continue;   // one build above 256 threads
           velo_options o = b0;
           o.launch_mode = mode;
           o.register_ctas = regs;
@@ -846,7 +968,7 @@ velo_status velo_fetch_staged(velo_ctx* c, uint8_t* buf, uint64_t size) {
 }
 
 velo_status velo_set_mlp(velo_ctx* c, const float* weights, float keep_threshold, float window_margin,
-                         float min_keep_rate) {
+                         float min_keep_rate, uint32_t max_event_hits) {
   if (!c || !weights) return VELO_ERR_INVALID_ARGUMENT;
   VELO_CUDA(c, cudaSetDevice(c->device));
   velo_status st = ensure(c, c->d_mlp, sizeof(float) * VELO_MLP_PARAMS, "mlp");
@@ -857,6 +979,9 @@ velo_status velo_set_mlp(velo_ctx* c, const float* weights, float keep_threshold
   c->keep_threshold = keep_threshold;
   c->window_margin = window_margin;
   c->min_keep_rate = min_keep_rate;
+  c->learned_max_hits = max_event_hits;
+  c->h_mlp.assign(weights, weights + VELO_MLP_PARAMS);
+  c->mlp_version++;
   c->mlp_set = true;
   return VELO_OK;
 }

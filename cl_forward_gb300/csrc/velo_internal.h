@@ -42,7 +42,19 @@ constexpr int kMlpB2 = kMlpW2 + kMlpHidden * kMlpHidden;
 constexpr int kMlpW3 = kMlpB2 + kMlpHidden;
 constexpr int kMlpB3 = kMlpW3 + kMlpOut * kMlpHidden;
 static_assert(kMlpB3 + kMlpOut == VELO_MLP_PARAMS, "MLP parameter count");
-constexpr uint32_t kMlpSmemBytes = (VELO_MLP_PARAMS * 4 + 15) & ~15;
+
+// The same weights in FP16 tensor-core fragment order for inference
+// (velo_mlp_warp.cuh): B fragments of W1^T (K 16 x N 32), W2^T (K 32 x N 32)
+// and W3^T (K 32 x N 8, 2 used) per n-tile and lane, biases in FP32.  Leads
+// the dynamic shared memory of a learned launch.
+struct alignas(8) MlpPair {
+  uint32_t x, y;
+};
+struct MlpFrag {
+  MlpPair w1[4][32], w2[2][4][32], w3[2][32];
+  float b1[kMlpHidden], b2[kMlpHidden], b3[8];
+};
+constexpr uint32_t kMlpSmemBytes = (sizeof(MlpFrag) + 15) & ~15u;
 
 // Per-event working set ("arena"): staged in dynamic shared memory when it
 // fits the launch's shared-memory size, else carved from global scratch.
@@ -113,6 +125,7 @@ struct SearchParams {
   float keep_threshold;
   float window_margin;
   float min_keep_rate;
+  uint32_t learned_max_hits;      // larger events take the plain method (0 = no limit)
 };
 
 // Launches the search kernel (velo_kernels.cu); reg_ctas (4 or 5) picks the

@@ -39,6 +39,7 @@
 #include <mutex>
 
 #include "velo_internal.h"
+#include "velo_mlp_warp.cuh"
 
 namespace velo {
 
@@ -79,7 +80,7 @@ struct EventView {
   velo_track* tracks;
   bool narrow;
   int event;
-  const float* mlp;         // learned seeding: weights in shared memory
+  const MlpFrag* mlp;       // learned seeding: weights in shared memory
   float keep_threshold, window_margin;
   float* dump_features;     // training-data dump
   uint32_t* dump_ids;
@@ -367,30 +368,6 @@ __device__ __forceinline__ void doublet_features(float* f, float h0x, float h0y,
   f[9] = fabsf(h1y - h0y) / dymax;
 }
 
-// The 10 -> 32 -> 32 -> 2 MLP on one doublet, weights in shared memory.
-__device__ __forceinline__ void mlp_eval(const float* __restrict__ w, const float* x, float* logit, float* width) {
-  float a1[kMlpHidden];
-#pragma unroll
-  for (int j = 0; j < kMlpHidden; ++j) {
-    float acc = w[kMlpB1 + j];
-#pragma unroll
-    for (int i = 0; i < kMlpIn; ++i) acc += w[kMlpW1 + j * kMlpIn + i] * x[i];
-    a1[j] = fmaxf(acc, 0.f);
-  }
-  float z = w[kMlpB3], wd = w[kMlpB3 + 1];
-#pragma unroll 4
-  for (int j = 0; j < kMlpHidden; ++j) {
-    float acc = w[kMlpB2 + j];
-#pragma unroll
-    for (int i = 0; i < kMlpHidden; ++i) acc += w[kMlpW2 + j * kMlpHidden + i] * a1[i];
-    acc = fmaxf(acc, 0.f);
-    z += w[kMlpW3 + j] * acc;
-    wd += w[kMlpW3 + kMlpHidden + j] * acc;
-  }
-  *logit = z;
-  *width = wd;
-}
-
 constexpr int kPlain = 0;    // the reference's seeding
 constexpr int kDump = 1;     // plain, recording sampled doublets as training data
 constexpr int kLearned = 2;  // MLP-pruned seeding
@@ -454,8 +431,8 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
       float tol = kTolerance;
       if constexpr (kMode != kPlain) {
         bool keep = cand;
+        float feat[kMlpIn];
         if (cand) {
-          float feat[kMlpIn];
           doublet_features(feat, h0x, h0y, h0z, h1x, h1y, h1z, f, ev.S, 0.5f * (zmin4 + zmax4), b - a, dymax);
           if constexpr (kMode == kDump) {
             uint32_t hs = (uint32_t)ev.event * 0x9E3779B1u ^ (uint32_t)h0 * 0x85EBCA77u ^ (uint32_t)h1 * 0xC2B2AE3Du;
@@ -472,14 +449,20 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
                 ev.dump_ids[3 * k + 2] = (uint32_t)h1;
               }
             }
-          } else {
-            float logit, width;
-            mlp_eval(ev.mlp, feat, &logit, &width);
-            keep = logit >= ev.keep_threshold;
-            tol = fminf(kTolerance, fmaxf(width, 0.f) + ev.window_margin);
           }
         }
-        if constexpr (kMode == kLearned) {           // keep-rate bookkeeping for the guard
+        if constexpr (kMode == kLearned) {
+          if (__any_sync(kFull, cand)) {             // the warp scores its 32 doublets together
+            if (!cand) {
+#pragma unroll
+              for (int q = 0; q < kMlpIn; ++q) feat[q] = 0.f;
+            }
+            float logit, width;
+            mlp_eval_warp(*ev.mlp, feat, &logit, &width);
+            keep = cand && logit >= ev.keep_threshold;
+            tol = fminf(kTolerance, fmaxf(width, 0.f) + ev.window_margin);
+          }
+          // keep-rate bookkeeping for the guard
           const unsigned mc = __ballot_sync(kFull, cand), mk = __ballot_sync(kFull, cand && keep);
           if (lane == 0 && mc) {
             atomicAdd(&s.considered, (uint32_t)__popc(mc));
@@ -576,7 +559,7 @@ __device__ unsigned long long g_phase_cycles[8];
 
 // ---------------------------------------------------------------------------
 template <int kMode>
-__device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* dyn, const float* mlp_smem) {
+__device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* dyn, const MlpFrag* mlp_smem) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   VELO_PHASE_BEGIN();
@@ -708,8 +691,8 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   // The learned seeding runs first when enabled; if it kept too small a
   // fraction of the doublets it scored, the event is searched again by the
   // plain method (used flags and lists reset; windows kept).
-  bool learned = kMode == kLearned;
-  uint32_t fallback = 0;
+  bool learned = kMode == kLearned && (p.learned_max_hits == 0 || (uint32_t)H <= p.learned_max_hits);
+  uint32_t fallback = (kMode == kLearned && !learned) ? VELO_EVENT_LEARNED_FALLBACK : 0u;
   for (int attempt = 0; attempt < 2; ++attempt) {
     if (attempt > 0) {
       for (int i = tid; i < H; i += nt) ev.used[i] = 0;
@@ -814,11 +797,11 @@ __global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const Sea
   extern __shared__ __align__(16) uint8_t dyn_smem_raw[];
   __shared__ Shared s;
   // learned seeding: the MLP weights lead the dynamic shared memory
-  const float* mlp_smem = nullptr;
+  const MlpFrag* mlp_smem = nullptr;
   uint8_t* dyn_smem = dyn_smem_raw;
   if constexpr (kMode == kLearned) {
-    float* w = reinterpret_cast<float*>(dyn_smem_raw);
-    for (int i = threadIdx.x; i < VELO_MLP_PARAMS; i += blockDim.x) w[i] = p.mlp[i];
+    MlpFrag* w = reinterpret_cast<MlpFrag*>(dyn_smem_raw);
+    stage_mlp_fragments(p.mlp, w);
     __syncthreads();
     mlp_smem = w;
     dyn_smem = dyn_smem_raw + kMlpSmemBytes;

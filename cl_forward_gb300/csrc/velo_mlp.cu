@@ -1,5 +1,7 @@
-// velo_mlp.cu -- the doublet scorer: a 10 -> 32 -> 32 -> 2 ReLU MLP in FP32,
-// trained with hand-written forward / backward / Adam kernels.
+// velo_mlp.cu -- the doublet scorer: a 10 -> 32 -> 32 -> 2 ReLU MLP trained in
+// FP32 with hand-written forward / backward / Adam kernels; inference
+// (velo_mlp_forward and the learned seeding) runs in FP16 on the tensor cores
+// (velo_mlp_warp.cuh).
 //
 // Outputs per (h0, h1) doublet: a keep logit and the half-width (mm) of the
 // x window around the straight-line prediction at module f-4 in which the
@@ -18,6 +20,7 @@
 #include <vector>
 
 #include "velo_internal.h"
+#include "velo_mlp_warp.cuh"
 
 namespace velo {
 
@@ -150,19 +153,24 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
   w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-__global__ void mlp_forward_kernel(const float* __restrict__ w, const float* __restrict__ x, int64_t n,
-                                   float* __restrict__ out) {
-  __shared__ float sw[VELO_MLP_PARAMS];
-  for (int i = threadIdx.x; i < VELO_MLP_PARAMS; i += blockDim.x) sw[i] = w[i];
+// Inference as the learned seeding does it (FP16 tensor-core MMA, one warp
+// per 32 samples), so the threshold calibrated on its outputs is the one the
+// search applies.
+__global__ void __launch_bounds__(256) mlp_forward_kernel(const float* __restrict__ w, const float* __restrict__ x,
+                                                          int64_t n, float* __restrict__ out) {
+  __shared__ MlpFrag frag;
+  stage_mlp_fragments(w, &frag);
   __syncthreads();
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  float xi[kMlpIn], a1[kMlpHidden], a2[kMlpHidden], o[kMlpOut];
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;   // whole warps stay in the kernel
+  float xi[kMlpIn];
 #pragma unroll
-  for (int i = 0; i < kMlpIn; ++i) xi[i] = x[k * kMlpIn + i];
-  mlp_forward_sample(sw, xi, a1, a2, o);
-  out[2 * k] = o[0];
-  out[2 * k + 1] = o[1];
+  for (int i = 0; i < kMlpIn; ++i) xi[i] = k < n ? x[k * kMlpIn + i] : 0.f;
+  float logit, width;
+  mlp_eval_warp(frag, xi, &logit, &width);
+  if (k < n) {
+    out[2 * k] = logit;
+    out[2 * k + 1] = width;
+  }
 }
 
 namespace {

@@ -58,6 +58,17 @@ def forward_np(w: np.ndarray, x: np.ndarray) -> np.ndarray:
     return h2 @ C.T + c
 
 
+def forward_fp16_np(w: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """The inference arithmetic of the GPU (velo_mlp_forward, learned seeding):
+    features, weights and hidden activations rounded to FP16, sums in FP32
+    or wider, biases in FP32."""
+    A, a, B, b, C, c = unpack(w)
+    h = lambda v: np.asarray(v, np.float32).astype(np.float16).astype(np.float64)
+    h1 = np.maximum(h(x) @ h(A).T + a, 0)
+    h2 = np.maximum(h(h1) @ h(B).T + b, 0)
+    return h(h2) @ h(C).T + c
+
+
 def reference_loss_and_grad(w: np.ndarray, x: np.ndarray, label: np.ndarray, target: np.ndarray):
     """Mean loss and its gradient in float64 (the CPU check of the CUDA kernels)."""
     A, a, B, b, C, c = unpack(w)
@@ -198,7 +209,7 @@ def _chunks(n, size):
     return [(a, min(n, a + size)) for a in range(0, n, size)]
 
 
-def compare_paths(ctx, blobs, truths, weights, thr, margin, min_keep, options, chunk=10000, iters=3):
+def compare_paths(ctx, blobs, truths, weights, thr, margin, min_keep, options, chunk=10000, iters=3, max_hits=0):
     """Plain vs learned over ``blobs`` in chunks: events/s (device time), rates, fallbacks."""
     from .validation import Rates, rates_fast
     out = {}
@@ -211,7 +222,7 @@ def compare_paths(ctx, blobs, truths, weights, thr, margin, min_keep, options, c
             buf, offs, sizes = pack_events(sub)
             ctx.stage(buf, offs, sizes)
             if learned_flag:
-                ctx.set_mlp(weights, thr, margin, min_keep)
+                ctx.set_mlp(weights, thr, margin, min_keep, max_hits)
             ms = sorted(ctx.time_runs(o, warmup=1 if i == 0 else 0, iters=1, flush_l2=True) for i in range(iters))
             total_ms += ms[len(ms) // 2]
             ctx.run(o)
@@ -246,6 +257,8 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--recall", type=float, default=0.999)
     ap.add_argument("--min-keep-rate", type=float, default=0.02)
+    ap.add_argument("--max-hits-factor", type=float, default=1.0,
+                    help="events above this x the largest training event take the plain method")
     ap.add_argument("--out", default="learned_out")
     a = ap.parse_args(argv)
     os.makedirs(a.out, exist_ok=True)
@@ -260,6 +273,8 @@ def main(argv=None):
     parts = []
     for lo, hi in _chunks(len(train_blobs), 10000):
         parts.append(build_dataset(ctx, train_blobs[lo:hi], keep_one_in=a.keep_one_in, capacity=4_000_000))
+    train_hits = np.array([int(np.frombuffer(b[4:8], "<i4")[0]) for b in train_blobs])
+    max_hits = int(a.max_hits_factor * train_hits.max())
     ds = Dataset(np.concatenate([p.x for p in parts]), np.concatenate([p.label for p in parts]),
                  np.concatenate([p.target for p in parts]), len(train_blobs))
     cal = build_dataset(ctx, calib_blobs, keep_one_in=1, capacity=20_000_000)
@@ -273,24 +288,27 @@ def main(argv=None):
     thr0, _ = calibrate(w0, cal, recall=a.recall)
     kept0 = keep_fraction(w0, cal, thr0)
     base = native.default_options(launch_mode=1, threads_per_event=128, smem_hits=600, register_ctas=4)
-    res4 = compare_paths(ctx, held_blobs, held_truths, w, thr, margin, a.min_keep_rate, base)
+    res4 = compare_paths(ctx, held_blobs, held_truths, w, thr, margin, a.min_keep_rate, base, max_hits=max_hits)
     report = {"config4": {"train_events": len(train_blobs), "train_doublets": int(len(ds.x)),
                           "train_positive": int(ds.label.sum()), "steps": a.steps, "batch": 4096, "lr": 1e-3,
                           "train_seconds": train_s, "loss_first": float(losses[:50].mean()),
                           "loss_last": float(losses[-50:].mean()), "keep_threshold": thr, "window_margin": margin,
                           "kept_fraction": kept, "kept_fraction_untrained": kept0,
+                          "max_event_hits": max_hits, "train_hits_mean": float(train_hits.mean()),
                           "heldout_events": len(held_blobs), "results": res4}}
     print(json.dumps(report["config4"]["results"]["delta"]), flush=True)
     np.savez(os.path.join(a.out, "doublet_mlp.npz"), weights=w, keep_threshold=np.float32(thr),
              window_margin=np.float32(margin), min_keep_rate=np.float32(a.min_keep_rate),
-             sha256=hashlib.sha256(w.tobytes()).hexdigest())
+             max_event_hits=np.uint32(max_hits), sha256=hashlib.sha256(w.tobytes()).hexdigest())
     del train_blobs, ds
     if a.stress_events:
         sb, st = _sorted_events(range(3000000, 3000000 + a.stress_events), generator.CONFIG_STRESS)
-        res5 = compare_paths(ctx, sb, st, w, thr, margin, a.min_keep_rate, base)
+        res5 = compare_paths(ctx, sb, st, w, thr, margin, a.min_keep_rate, base, max_hits=max_hits)
+        res5_open = compare_paths(ctx, sb, st, w, thr, margin, a.min_keep_rate, base, max_hits=0)
         report["config5"] = {"events": len(sb), "mean_hits": float(np.mean([int(np.frombuffer(b[4:8], "<i4")[0])
-                                                                             for b in sb])), "results": res5}
-        print(json.dumps(res5["delta"]), flush=True)
+                                                                             for b in sb])), "results": res5,
+                             "results_without_hits_guard": res5_open}
+        print(json.dumps(res5["delta"]), json.dumps(res5_open["delta"]), flush=True)
     with open(os.path.join(a.out, "learned_report.json"), "w") as f:
         json.dump(report, f, indent=1)
     print(f"done in {time.time() - t0:.0f}s", flush=True)

@@ -66,7 +66,8 @@ class Options(ctypes.Structure):
                 ("launch_mode", ctypes.c_int32), ("smem_hits", ctypes.c_int32),
                 ("narrow_windows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("register_ctas", ctypes.c_int32),
-                ("learned", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("learned", ctypes.c_int32), ("pipeline_events", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 class Stats(ctypes.Structure):
@@ -129,7 +130,7 @@ def load() -> ctypes.CDLL:
     l.velo_autotune.argtypes = [vp, ctypes.POINTER(Options), i32, ctypes.POINTER(Options),
                                 ctypes.POINTER(ctypes.c_float)]
     f32 = ctypes.c_float
-    l.velo_set_mlp.argtypes = [vp, vp, f32, f32, f32]
+    l.velo_set_mlp.argtypes = [vp, vp, f32, f32, f32, ctypes.c_uint32]
     l.velo_dump_doublets.argtypes = [vp, ctypes.POINTER(Options), ctypes.c_uint32, vp, vp, u64,
                                      ctypes.POINTER(u64)]
     l.velo_mlp_train.argtypes = [vp, vp, vp, ctypes.c_int64, i32, i32, f32, u64, vp, vp]
@@ -272,11 +273,12 @@ class Context:
                     "velo_autotune")
         return best, float(ms.value)
 
-    def set_mlp(self, weights: np.ndarray, keep_threshold: float, window_margin: float, min_keep_rate: float):
+    def set_mlp(self, weights: np.ndarray, keep_threshold: float, window_margin: float, min_keep_rate: float,
+                max_event_hits: int = 0):
         w = np.ascontiguousarray(weights, np.float32)
         assert w.size == MLP_PARAMS
-        self._check(self._lib.velo_set_mlp(self._h, _p(w), keep_threshold, window_margin, min_keep_rate),
-                    "velo_set_mlp")
+        self._check(self._lib.velo_set_mlp(self._h, _p(w), keep_threshold, window_margin, min_keep_rate,
+                                           int(max_event_hits)), "velo_set_mlp")
 
     def dump_doublets(self, capacity: int, keep_one_in: int = 1, options: Optional[Options] = None):
         """Features and {event, h0, h1} of sampled doublets of a plain run on the staged events."""

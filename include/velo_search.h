@@ -71,7 +71,8 @@ typedef enum velo_status {
 #define VELO_EVENT_MAX_TRACKS 0x4u      /* more than MAX_TRACKS tracks (Kernel.cl:336,810) */
 #define VELO_EVENT_INVALID 0x8u         /* blob failed validation; no tracks */
 #define VELO_EVENT_DEGENERATE 0x10u     /* an inf/NaN fit (two modules' hits at equal z) */
-#define VELO_EVENT_LEARNED_FALLBACK 0x20u  /* learned seeding kept too few doublets; rerun plain */
+#define VELO_EVENT_LEARNED_FALLBACK 0x20u  /* learned seeding not trusted (too few doublets kept, or
+                                              more hits than max_event_hits): plain method */
 
 typedef enum velo_launch_mode {
   VELO_LAUNCH_PER_EVENT = 0,   /* one CTA per event (the reference's one work-group per event) */
@@ -90,7 +91,11 @@ typedef struct velo_options {
                                  CTAs per SM (fewer registers, more CTAs); 0 = 5 */
   int32_t learned;            /* 1: seeding prunes doublets with the MLP set by velo_set_mlp
                                  (approximate; no counterpart in the reference) */
-  int32_t reserved[7];
+  int32_t pipeline_events;    /* velo_search / velo_search_packed: > 0 cuts a batch of more than
+                                 twice this many events into parts of this size whose copies
+                                 and searches overlap on two streams (same results); the
+                                 context then holds no staged batch afterwards.  0 = off */
+  int32_t reserved[6];
 } velo_options;
 
 typedef struct velo_stats {
@@ -194,16 +199,18 @@ velo_status velo_autotune(velo_ctx* ctx, const velo_options* base, int32_t iters
  * position.  Doublets whose logit is below keep_threshold are skipped; the
  * others search h2 only within half-width + window_margin (never wider than
  * the exact cut).  An event whose kept fraction of doublets falls below
- * min_keep_rate is re-searched by the plain method and flagged
- * VELO_EVENT_LEARNED_FALLBACK.  Parameters: W1[32][10] b1[32] W2[32][32]
- * b2[32] W3[2][32] b3[2], FP32.
+ * min_keep_rate is re-searched by the plain method, and an event with more
+ * than max_event_hits hits (outside the range the network was trained on;
+ * 0 = no limit) is searched by the plain method from the start; both are
+ * flagged VELO_EVENT_LEARNED_FALLBACK.  Parameters: W1[32][10] b1[32]
+ * W2[32][32] b2[32] W3[2][32] b3[2], FP32 (inference rounds them to FP16).
  */
 #define VELO_MLP_INPUTS 10
 #define VELO_MLP_HIDDEN 32
 #define VELO_MLP_OUTPUTS 2
 #define VELO_MLP_PARAMS 1474
 velo_status velo_set_mlp(velo_ctx* ctx, const float* weights, float keep_threshold, float window_margin,
-                         float min_keep_rate);
+                         float min_keep_rate, uint32_t max_event_hits);
 
 /* Training data: runs the plain search on the staged events and records,
  * for one in `keep_one_in` of the doublets that reach the h2 search (hashed
@@ -249,7 +256,7 @@ int32_t velo_device_sm_count(const velo_ctx* ctx);
  * NULL = the legacy default stream) and the results are valid once it is
  * synchronised.  Y-lanes as in velo_options; narrowing is on.
  *
- * All other memory is one file-scope device array of about 15 MB per GPU,
+ * All other memory is one file-scope device array of about 16 MB per GPU,
  * held from library load to process exit.  Limits per call, rejected with
  * VELO_ERR_CAPACITY: n_events <= VELO_STATIC_MAX_EVENTS;
  * total_hits + n_events <= VELO_STATIC_MAX_HIT_ROWS (total_hits = the sum of

@@ -33,8 +33,21 @@ def test_mlp_gradients_match_cpu(native_lib):
     assert abs(loss - loss_ref) <= 1e-5 * max(1.0, abs(loss_ref))
     scale = np.abs(g_ref).max()
     assert np.max(np.abs(g - g_ref)) <= 2e-4 * scale + 1e-7
-    out = native.mlp_forward(w, x)
-    assert np.allclose(out, learned.forward_np(w, x), rtol=1e-4, atol=1e-5)
+
+def test_mlp_inference_matches_fp16_restatement(native_lib):
+    """Tensor-core inference (FP16 operands, FP32 sums) against the same
+    rounding done in numpy, and within FP16 error of the FP32 network.  The
+    tolerance allows one FP16 rounding of a hidden unit to land on the other
+    side (2^-11 relative) through the following layers."""
+    from cl_forward_gb300 import learned, native
+    for seed in (5, 6):
+        w = learned.init_weights(seed)
+        x, _, _ = _data(5001, seed)          # a partial last warp
+        out = native.mlp_forward(w, x)
+        ref16 = learned.forward_fp16_np(w, x)
+        scale = 1.0 + np.abs(ref16)
+        assert np.max(np.abs(out - ref16) / scale) < 2e-3
+        assert np.max(np.abs(out - learned.forward_np(w, x)) / scale) < 3e-2
 
 
 def test_training_reduces_loss(native_lib):
@@ -75,6 +88,19 @@ def test_learned_with_nothing_pruned_equals_plain(gpu_ctx, oracle_lib):
     assert np.all(status & native.EVENT_LEARNED_FALLBACK)
     for e in range(len(blobs)):
         assert index_lists(got[e]) == index_lists(want[e])
+    # events above the hit-count limit take the plain method from the start
+    hits = np.array([int(np.frombuffer(b[4:8], "<i4")[0]) for b in blobs])
+    limit = int(np.median(hits))
+    gpu_ctx.set_mlp(learned.init_weights(0), keep_threshold=1e30, window_margin=0.0, min_keep_rate=0.0,
+                    max_event_hits=limit)
+    got, status = gpu_ctx.search(blobs, native.default_options(learned=1))
+    over = hits > limit
+    assert over.any() and (~over).any()
+    assert np.array_equal((status & native.EVENT_LEARNED_FALLBACK) != 0, over)
+    for e in np.flatnonzero(over):
+        assert index_lists(got[e]) == index_lists(want[e])
+    for e in np.flatnonzero(~over):          # everything pruned: no seeds, no tracks
+        assert len(got[e]) == 0
 
 
 def test_trained_network_gains_over_untrained(gpu_ctx, oracle_lib):

@@ -246,3 +246,26 @@ def test_track_fits_match_least_squares(gpu_ctx, oracle_lib):
             assert abs(f["chi2_ndf"] - chi2) <= 1e-3 * max(chi2, 1e-3) + 1e-4
             checked += 1
     assert checked > 1000
+
+
+@pytest.mark.parametrize("part,mode", [(128, 0), (100, 1)])
+def test_pipelined_search_matches_one_launch(gpu_ctx, oracle_lib, part, mode):
+    """Batches cut into overlapped parts on two streams: the same tracks per
+    event, first[] rebased into one output array, statuses and the strict
+    call's error for an invalid event kept."""
+    from cl_forward_gb300 import events, fuzz, generator, native
+    blobs = _sorted(oracle_lib, generator.generate(range(5000, 5650))[0])
+    blobs[333] = b"\x05\x00\x00\x00"                        # invalid, in a middle part
+    blobs[400] = fuzz.empty_event()
+    one, st1 = gpu_ctx.search(blobs, native.default_options(launch_mode=mode), allow_invalid=True)
+    piped, st2 = gpu_ctx.search(blobs, native.default_options(launch_mode=mode, pipeline_events=part),
+                                allow_invalid=True)
+    assert np.array_equal(st1, st2) and st2[333] & native.EVENT_INVALID
+    for e in range(len(blobs)):
+        assert index_lists(piped[e]) == index_lists(one[e])
+    s = gpu_ctx.stats()
+    assert s.launches == -(-len(blobs) // part) and s.total_tracks == sum(len(t) for t in piped)
+    with pytest.raises(native.VeloError):
+        gpu_ctx.search(blobs, native.default_options(pipeline_events=part))
+    with pytest.raises(native.VeloError):                   # the parent holds no staged batch afterwards
+        gpu_ctx.fit_tracks(16)
