@@ -73,6 +73,8 @@ def parse_args():
     ap.add_argument("--e2e-chunk", type=int, default=16000, help="events per end-to-end call")
     ap.add_argument("--e2e-pipeline", type=int, default=2500,
                     help="events per overlapped part inside an end-to-end call (0: one part)")
+    ap.add_argument("--e2e-copies", action="store_true",
+                    help="end-to-end: stage copies instead of reading / writing pinned host buffers in place")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-pruning leg")
@@ -422,6 +424,7 @@ def gpu_arm(args, ranks: Ranks):
 
     e2e_opts = native.Options.from_buffer_copy(opts)
     e2e_opts.pipeline_events = args.e2e_pipeline
+    e2e_opts.host_direct = 0 if args.e2e_copies else 1
 
     def e2e_pass():
         for a, b in bounds:
@@ -461,6 +464,9 @@ def gpu_arm(args, ranks: Ranks):
                    "register_ctas": opts.register_ctas, "cuda_graph": bool(opts.use_graph),
                    "smem_hits_option": opts.smem_hits, "autotuned": tuned,
                    "e2e_chunk_events": chunk, "e2e_pipeline_events": args.e2e_pipeline,
+                   "e2e_io": ("H2D / D2H copies" if args.e2e_copies else
+                              "events read and tracks written in place in pinned host memory by the kernel "
+                              "(NVLink-C2C); per-event counts / offsets / status copied"),
                    "l2": "flushed between timed steps (2 x L2 memset); input also larger than L2",
                    "parallelism": f"weak scaling over {args.gpus} GPU(s), event blocks per rank"},
         "impl": "gb300",

@@ -45,7 +45,7 @@ struct velo_ctx {
   std::vector<uint64_t> h_offset;
   std::vector<uint32_t> h_hits, h_maxmod, h_valid;
   std::vector<uint64_t> h_hit_base;
-  std::vector<uint32_t> h_status;
+  std::vector<uint32_t> h_status, h_counts;
   uint64_t rows = 0;
   uint64_t input_bytes = 0;
   uint64_t total_hits = 0;
@@ -73,6 +73,13 @@ struct velo_ctx {
   uint32_t learned_max_hits = 0;   // 0: no limit
   std::vector<float> h_mlp;        // host copy, handed on to the pipeline contexts
   uint64_t mlp_version = 0;
+
+  // in-place host I/O of the current batch (velo_options.host_direct):
+  // device-visible addresses of the caller's pinned buffers, null = copied
+  const uint8_t* io_input = nullptr;
+  velo_track* io_tracks = nullptr;
+  uint64_t io_capacity = 0;
+  unsigned long long* io_cursor = nullptr;   // output cursor shared by pipelined parts
 
   // pipelined searches (velo_options.pipeline_events): two child contexts,
   // each with its own stream and buffers, that alternate over the parts
@@ -311,10 +318,44 @@ const char* velo_last_error(const velo_ctx* c) { return c ? c->err.c_str() : "no
 
 int32_t velo_device_sm_count(const velo_ctx* c) { return c ? c->sm_count : 0; }
 
+namespace {
+
+// Device-visible address of host memory the GPU can access in place (pinned
+// memory mapped into the device's address space); null for anything else.
+void* device_view(const void* host) {
+  if (!host) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();   // clear the (non-sticky) error of an unknown pointer
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+  return a.devicePointer;
+}
+
+velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
+                       int32_t n, bool direct);
+
+}  // namespace
+
 velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
                        int32_t n) {
+  if (!c) return VELO_ERR_INVALID_ARGUMENT;
+  c->io_tracks = nullptr;
+  c->io_capacity = 0;
+  c->io_cursor = nullptr;
+  return stage_impl(c, buf, offsets, sizes, n, false);
+}
+
+namespace {
+
+// Stages a batch: host checks, per-event metadata, and the events themselves
+// (copied, or with `direct` read in place when buf is mapped pinned memory).
+velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
+                       int32_t n, bool direct) {
   if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
   VELO_CUDA(c, cudaSetDevice(c->device));
+  c->io_input = nullptr;
   c->staged = false;
   c->meta_valid = false;
   c->ran = false;
@@ -355,7 +396,8 @@ velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   c->total_hits = hits;
   c->input_bytes = hi - lo;
   velo_status st;
-  if ((st = ensure(c, c->d_input, hi - lo + 16, "input")) != VELO_OK) return st;
+  if (direct && hi > lo) c->io_input = static_cast<const uint8_t*>(device_view(buf + lo));
+  if (!c->io_input && (st = ensure(c, c->d_input, hi - lo + 16, "input")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_offset, 8ull * n, "offsets")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_hits, 4ull * n, "hits")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_maxmod, 4ull * n, "maxmod")) != VELO_OK) return st;
@@ -369,7 +411,7 @@ velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   if ((st = ensure(c, c->d_out_first, 8ull * n, "first")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_out_status, 4ull * n, "status")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_counters, 64, "counters")) != VELO_OK) return st;
-  if (hi > lo)
+  if (hi > lo && !c->io_input)
     VELO_CUDA(c, cudaMemcpyAsync(c->d_input.p, buf + lo, hi - lo, cudaMemcpyHostToDevice, c->stream));
   if (n > 0) {
     VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_offset.p, c->h_offset.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
@@ -381,6 +423,8 @@ velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   c->staged = true;
   return VELO_OK;
 }
+
+}  // namespace
 
 namespace {
 
@@ -528,7 +572,7 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
   VELO_CUDA(c, cudaMemsetAsync(c->d_counters.p, 0, 64, c->stream));
   if (c->n == 0) return VELO_OK;
   velo::SearchParams p{};
-  p.input = P<uint8_t>(c->d_input);
+  p.input = c->io_input ? c->io_input : P<uint8_t>(c->d_input);
   p.ev_offset = P<uint64_t>(c->d_ev_offset);
   p.ev_hits = P<uint32_t>(c->d_ev_hits);
   p.ev_maxmod = P<uint32_t>(c->d_ev_maxmod);
@@ -545,11 +589,12 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
   p.tracklets = P<uint32_t>(c->d_tracklets);
   p.weak = P<uint32_t>(c->d_weak);
   p.tracks = P<velo_track>(c->d_tracks);
-  p.out_tracks = P<velo_track>(c->d_out_tracks);
+  p.out_tracks = c->io_tracks ? c->io_tracks : P<velo_track>(c->d_out_tracks);
+  p.out_capacity = c->io_tracks ? c->io_capacity : c->rows;
   p.out_counts = P<uint32_t>(c->d_out_counts);
   p.out_first = P<uint64_t>(c->d_out_first);
   p.out_status = P<uint32_t>(c->d_out_status);
-  p.out_cursor = P<unsigned long long>(c->d_counters);
+  p.out_cursor = c->io_cursor ? c->io_cursor : P<unsigned long long>(c->d_counters);
   p.work_counter = reinterpret_cast<int32_t*>(P<uint8_t>(c->d_counters) + 32);
   if (o.learned) {
     p.mlp = P<float>(c->d_mlp);
@@ -645,7 +690,8 @@ velo_status velo_fetch(velo_ctx* c, velo_track* tracks_out, uint64_t capacity, u
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, c->e0, c->e1) == cudaSuccess) c->stats.kernel_ms = ms;
   unsigned long long total = 0;
-  VELO_CUDA(c, cudaMemcpyAsync(&total, c->d_counters.p, 8, cudaMemcpyDeviceToHost, c->stream));
+  if (!c->io_cursor)
+    VELO_CUDA(c, cudaMemcpyAsync(&total, c->d_counters.p, 8, cudaMemcpyDeviceToHost, c->stream));
   if (c->n > 0) {
     if (counts)
       VELO_CUDA(c, cudaMemcpyAsync(counts, c->d_out_counts.p, 4ull * c->n, cudaMemcpyDeviceToHost, c->stream));
@@ -654,11 +700,28 @@ velo_status velo_fetch(velo_ctx* c, velo_track* tracks_out, uint64_t capacity, u
     c->h_status.resize(c->n);
     VELO_CUDA(c, cudaMemcpyAsync(c->h_status.data(), c->d_out_status.p, 4ull * c->n,
                                  cudaMemcpyDeviceToHost, c->stream));
+    if (c->io_cursor && !counts) {
+      c->h_counts.resize(c->n);
+      VELO_CUDA(c, cudaMemcpyAsync(c->h_counts.data(), c->d_out_counts.p, 4ull * c->n,
+                                   cudaMemcpyDeviceToHost, c->stream));
+    }
   }
   VELO_CUDA(c, cudaStreamSynchronize(c->stream));
   if (status && c->n > 0) std::memcpy(status, c->h_status.data(), 4ull * c->n);
+  if (c->io_cursor) {   // a part of a pipelined batch: its own tracks are the sum of its counts
+    const uint32_t* cn = counts ? counts : c->h_counts.data();
+    for (int32_t e = 0; e < c->n; ++e) total += cn[e];
+  }
   c->stats.total_tracks = total;
   c->stats.output_bytes = 4ull * c->n + sizeof(velo_track) * total;
+  if (c->io_tracks) {   // written in place by the kernel
+    if (!c->io_cursor && total > c->io_capacity) {
+      c->err = "track buffer holds " + std::to_string(c->io_capacity) + " tracks, " + std::to_string(total) +
+               " needed";
+      return VELO_ERR_CAPACITY;
+    }
+    return VELO_OK;
+  }
   if (tracks_out == nullptr && capacity == 0) return VELO_OK;
   if (total > capacity) {
     c->err = "track buffer holds " + std::to_string(capacity) + " tracks, " + std::to_string(total) + " needed";
@@ -711,6 +774,21 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
   c->staged = false;
   c->ran = false;
   c->generation++;
+  // in-place output: all parts reserve rows from one cursor in the caller's
+  // buffer, so first[] needs no rebasing
+  velo_track* direct_out =
+      (o.host_direct && tracks_out && capacity) ? static_cast<velo_track*>(device_view(tracks_out)) : nullptr;
+  if (direct_out) {
+    velo_status st = ensure(c, c->d_counters, 64, "counters");
+    if (st != VELO_OK) return st;
+    VELO_CUDA(c, cudaMemsetAsync(c->d_counters.p, 0, 64, c->stream));
+    VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  for (int k = 0; k < 2; ++k) {
+    c->pipe[k]->io_tracks = direct_out;
+    c->pipe[k]->io_capacity = direct_out ? capacity : 0;
+    c->pipe[k]->io_cursor = direct_out ? P<unsigned long long>(c->d_counters) : nullptr;
+  }
   const int32_t part = o.pipeline_events;
   const int32_t n_parts = (n + part - 1) / part;
   uint64_t base = 0, hits = 0, in_bytes = 0;
@@ -721,15 +799,15 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
     velo_ctx* ch = c->pipe[k & 1];
     const int32_t a = k * part, b = std::min(n, a + part);
     const bool want_tracks = tracks_out != nullptr || capacity != 0;
-    velo_status st = velo_fetch(ch, want_tracks ? tracks_out + base : nullptr,
-                                want_tracks ? (capacity > base ? capacity - base : 0) : 0,
+    velo_status st = velo_fetch(ch, want_tracks && !direct_out ? tracks_out + base : nullptr,
+                                want_tracks && !direct_out ? (capacity > base ? capacity - base : 0) : 0,
                                 counts ? counts + a : nullptr, first ? first + a : nullptr,
                                 status ? status + a : nullptr);
     if (st != VELO_OK) {
       c->err = ch->err;
       return st;
     }
-    if (first)
+    if (first && !direct_out)
       for (int32_t e = a; e < b; ++e) first[e] += base;
     for (int32_t e = a; e < b && bad_event < 0; ++e)
       if (ch->h_status[e - a] & VELO_EVENT_INVALID) bad_event = e;
@@ -744,7 +822,7 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
     if (first_error != VELO_OK) break;
     velo_ctx* ch = c->pipe[k & 1];
     const int32_t a = k * part, b = std::min(n, a + part);
-    velo_status st = velo_stage(ch, buf, offsets + a, sizes + a, b - a);
+    velo_status st = stage_impl(ch, buf, offsets + a, sizes + a, b - a, o.host_direct != 0);
     if (st == VELO_OK) st = velo_run(ch, &po);
     if (st != VELO_OK) {
       c->err = ch->err;
@@ -754,10 +832,32 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
   }
   // drain: the last two parts (and, after an error, whatever is in flight)
   for (int k = 0; k < 2; ++k) cudaStreamSynchronize(c->pipe[k]->stream);
-  if (first_error != VELO_OK) return first_error;
+  auto release = [&]() {   // the children pointed into the caller's buffers
+    for (int k = 0; k < 2; ++k) {
+      velo_ctx* ch = c->pipe[k];
+      ch->io_input = nullptr;
+      ch->io_tracks = nullptr;
+      ch->io_capacity = 0;
+      ch->io_cursor = nullptr;
+      ch->staged = false;
+      ch->ran = false;
+    }
+  };
+  if (first_error != VELO_OK) {
+    release();
+    return first_error;
+  }
   for (int32_t k = std::max(0, n_parts - 2); k < n_parts; ++k) {
     velo_status st = finish(k);
-    if (st != VELO_OK) return st;
+    if (st != VELO_OK) {
+      release();
+      return st;
+    }
+  }
+  release();
+  if (direct_out && base > capacity) {
+    c->err = "track buffer holds " + std::to_string(capacity) + " tracks, " + std::to_string(base) + " needed";
+    return VELO_ERR_CAPACITY;
   }
   c->stats.n_events = (uint32_t)n;
   c->stats.total_hits = hits;
@@ -786,6 +886,35 @@ velo_status velo_search_packed(velo_ctx* c, const uint8_t* buf, const uint64_t* 
     if (st != VELO_OK) return st;
     VELO_CUDA(c, cudaSetDevice(c->device));
     return search_pipelined(c, buf, offsets, sizes, n, o, tracks_out, capacity, counts, first, status);
+  }
+  if (opts && opts->host_direct) {
+    velo_options o;
+    velo_status st = check_options(c, opts, &o);
+    if (st != VELO_OK) return st;
+    VELO_CUDA(c, cudaSetDevice(c->device));
+    o.use_graph = 0;   // the buffers change from call to call
+    c->io_tracks = (tracks_out && capacity) ? static_cast<velo_track*>(device_view(tracks_out)) : nullptr;
+    c->io_capacity = c->io_tracks ? capacity : 0;
+    c->io_cursor = nullptr;
+    st = stage_impl(c, buf, offsets, sizes, n, true);
+    if (st == VELO_OK) st = velo_run(c, &o);
+    if (st == VELO_OK) st = velo_fetch(c, tracks_out, capacity, counts, first, status);
+    const bool in_place = c->io_input != nullptr || c->io_tracks != nullptr;
+    c->io_input = nullptr;
+    c->io_tracks = nullptr;
+    c->io_capacity = 0;
+    if (in_place) {   // the batch pointed into the caller's buffers
+      c->staged = false;
+      c->ran = false;
+      c->generation++;
+    }
+    if (st != VELO_OK) return st;
+    for (int32_t e = 0; e < n; ++e)
+      if (c->h_status[e] & VELO_EVENT_INVALID) {
+        c->err = "event " + std::to_string(e) + " failed validation";
+        return VELO_ERR_INVALID_EVENT;
+      }
+    return VELO_OK;
   }
   velo_status st = velo_stage(c, buf, offsets, sizes, n);
   if (st != VELO_OK) return st;

@@ -97,6 +97,7 @@ struct SearchParams {
   const uint64_t* hit_base;       // prefix sum of max(H, 1): per-event scratch row
   const uint64_t* arena_off;      // byte offset into global_arena, or kNoArena (shared memory)
   const int32_t* order;           // persistent mode: event processing order
+  uint64_t out_capacity;          // rows of out_tracks; rows past it are not written
   int32_t n_events;
   int32_t y_lanes;
   int32_t narrow;                 // 1 = binary-search narrowing of sorted modules

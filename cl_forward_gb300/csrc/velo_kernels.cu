@@ -780,7 +780,9 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   }
   __syncthreads();
   {
-    const uint32_t words = min(s.ntracks, ev.cap) * 25u;
+    // rows past out_capacity stay unwritten (the host reports the shortfall)
+    const unsigned long long room = s.out_first < p.out_capacity ? p.out_capacity - s.out_first : 0ull;
+    const uint32_t words = (uint32_t)min((unsigned long long)min(s.ntracks, ev.cap), room) * 25u;
     const uint32_t* src = reinterpret_cast<const uint32_t*>(ev.tracks);
     uint32_t* dst = reinterpret_cast<uint32_t*>(p.out_tracks + s.out_first);
     for (uint32_t w = tid; w < words; w += nt) dst[w] = src[w];

@@ -207,6 +207,7 @@ extern "C" velo_status velo_search_device_static(const uint8_t* d_input, const u
   p.weak = v.weak;
   p.tracks = v.tracks;
   p.out_tracks = d_tracks_out;
+  p.out_capacity = track_capacity;
   p.out_counts = d_counts;
   p.out_first = d_first;
   p.out_status = d_status;

@@ -95,7 +95,13 @@ typedef struct velo_options {
                                  twice this many events into parts of this size whose copies
                                  and searches overlap on two streams (same results); the
                                  context then holds no staged batch afterwards.  0 = off */
-  int32_t reserved[6];
+  int32_t host_direct;        /* velo_search_packed: 1 = when the event buffer and the track
+                                 buffer are pinned host memory (cudaHostAlloc/cudaHostRegister,
+                                 mapped), the kernel reads the events and writes the tracks in
+                                 place over the host link instead of staging copies; other
+                                 buffers are copied as usual.  Results are identical; the
+                                 context holds no staged batch afterwards.  0 = off */
+  int32_t reserved[5];
 } velo_options;
 
 typedef struct velo_stats {

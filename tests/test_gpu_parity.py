@@ -269,3 +269,39 @@ def test_pipelined_search_matches_one_launch(gpu_ctx, oracle_lib, part, mode):
         gpu_ctx.search(blobs, native.default_options(pipeline_events=part))
     with pytest.raises(native.VeloError):                   # the parent holds no staged batch afterwards
         gpu_ctx.fit_tracks(16)
+
+
+@pytest.mark.parametrize("part", [0, 96])
+def test_host_direct_io_matches_copies(gpu_ctx, oracle_lib, part):
+    """Events read and tracks written in place in pinned host memory (alone
+    and with pipelined parts) give the copied path's tracks; pageable buffers
+    fall back to copies; a short track buffer is reported, not overrun."""
+    from cl_forward_gb300 import events, fuzz, generator, native
+    blobs = _sorted(oracle_lib, generator.generate(range(6000, 6400))[0])
+    blobs[50] = fuzz.empty_event()
+    buf, offs, sizes = events.pack_events(blobs)
+    n = len(blobs)
+    cap = int(sum(max(int(np.frombuffer(b[4:8], "<i4")[0]), 1) for b in blobs))
+    pinned = gpu_ctx.host_alloc(len(buf))
+    pinned[:] = buf
+    ptracks = gpu_ctx.host_alloc(cap * 100).view(events.TRACK_DTYPE)
+    want, _ = oracle_lib.search(blobs, 4)
+    for src, dst in ((pinned, ptracks), (buf, np.zeros(cap, events.TRACK_DTYPE))):
+        for mode in (0, 1):
+            o = native.default_options(launch_mode=mode, host_direct=1, pipeline_events=part)
+            counts = np.zeros(n, np.uint32)
+            first = np.zeros(n, np.uint64)
+            status = np.zeros(n, np.uint32)
+            dst.view(np.uint8)[:] = 0
+            gpu_ctx.search_packed_into(src, offs, sizes, o, dst, counts, first, status)
+            assert not np.any(status & native.EVENT_INVALID)
+            for e in range(n):
+                assert index_lists(dst[int(first[e]):int(first[e]) + int(counts[e])]) == index_lists(want[e])
+            assert int((first + counts).max()) == int(counts.sum())          # one contiguous range
+    total = sum(len(t) for t in want)
+    with pytest.raises(native.VeloError):
+        o = native.default_options(host_direct=1, pipeline_events=part)
+        gpu_ctx.search_packed_into(pinned, offs, sizes, o, ptracks[:total - 1], np.zeros(n, np.uint32),
+                                   np.zeros(n, np.uint64), np.zeros(n, np.uint32))
+    gpu_ctx.host_free(pinned)
+    gpu_ctx.host_free(ptracks.view(np.uint8))
