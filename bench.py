@@ -71,7 +71,7 @@ def parse_args():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the library's default launch configuration instead of the autotuned one")
     ap.add_argument("--e2e-chunk", type=int, default=16000, help="events per end-to-end call")
-    ap.add_argument("--e2e-pipeline", type=int, default=2500,
+    ap.add_argument("--e2e-pipeline", type=int, default=0,
                     help="events per overlapped part inside an end-to-end call (0: one part)")
     ap.add_argument("--e2e-copies", action="store_true",
                     help="end-to-end: stage copies instead of reading / writing pinned host buffers in place")

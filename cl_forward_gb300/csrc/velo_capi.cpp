@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -23,6 +24,49 @@ namespace {
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
+};
+
+// Grow-only array in pinned host memory: the per-event metadata goes to the
+// device with asynchronous copies (a copy from pageable memory would first
+// wait for the stream, serialising the host behind the input transfer).
+template <typename T>
+struct PinnedVec {
+  T* p = nullptr;
+  size_t n = 0, cap = 0;
+  PinnedVec() = default;
+  PinnedVec(const PinnedVec&) = delete;
+  PinnedVec& operator=(const PinnedVec&) = delete;
+  ~PinnedVec() {
+    if (p) cudaFreeHost(p);
+  }
+  bool resize(size_t m) {
+    if (m > cap) {
+      T* q = nullptr;
+      const size_t nc = m + m / 4 + 64;
+      if (cudaHostAlloc(reinterpret_cast<void**>(&q), nc * sizeof(T), cudaHostAllocDefault) != cudaSuccess)
+        return false;
+      if (p) {
+        std::memcpy(q, p, n * sizeof(T));
+        cudaFreeHost(p);
+      }
+      p = q;
+      cap = nc;
+    }
+    n = m;
+    return true;
+  }
+  bool assign(size_t m, T v) {
+    if (!resize(m)) return false;
+    std::fill(p, p + m, v);
+    return true;
+  }
+  T* data() { return p; }
+  const T* data() const { return p; }
+  T* begin() { return p; }
+  T* end() { return p + n; }
+  T& operator[](size_t i) { return p[i]; }
+  const T& operator[](size_t i) const { return p[i]; }
+  size_t size() const { return n; }
 };
 
 }  // namespace
@@ -42,11 +86,13 @@ struct velo_ctx {
   // staged batch
   bool staged = false;
   int32_t n = 0;
-  std::vector<uint64_t> h_offset;
-  std::vector<uint32_t> h_hits, h_maxmod, h_valid;
-  std::vector<uint64_t> h_hit_base;
+  PinnedVec<uint64_t> h_offset;
+  PinnedVec<uint32_t> h_hits, h_maxmod, h_valid;
+  PinnedVec<uint64_t> h_hit_base;
+  cudaEvent_t meta_copied = nullptr;   // after the last copy out of the pinned metadata
   std::vector<uint32_t> h_status, h_counts;
   uint64_t rows = 0;
+  uint32_t max_modules = 0;   // largest S among the staged events
   uint64_t input_bytes = 0;
   uint64_t total_hits = 0;
 
@@ -56,8 +102,8 @@ struct velo_ctx {
   int meta_y = 0;
   int meta_persistent = -1;
   uint32_t configured_smem = 0;
-  std::vector<uint64_t> h_arena_off;
-  std::vector<int32_t> h_order;
+  PinnedVec<uint64_t> h_arena_off;
+  PinnedVec<int32_t> h_order;
   int32_t events_in_global = 0;
 
   void* h_stage = nullptr;
@@ -129,10 +175,34 @@ velo_status ensure(velo_ctx* c, DevBuf& b, size_t bytes, const char* what) {
 template <typename T>
 T* P(DevBuf& b) { return reinterpret_cast<T*>(b.p); }
 
+// Host wall time of a scope, written to *out (ms) when the scope ends.
+struct HostTimer {
+  float* out;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  explicit HostTimer(float* o) : out(o) {}
+  ~HostTimer() {
+    *out = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
 int32_t rd_i32(const uint8_t* p) {
   int32_t v;
   std::memcpy(&v, p, 4);
   return v;
+}
+
+// Header checks of the staging path: counts in range and the blob long
+// enough for them.  The module table (starts contiguous, counts adding up to
+// H) and the coordinates are checked by the search kernel, which marks a bad
+// event VELO_EVENT_INVALID, so the host reads 8 bytes per event.
+bool check_header(const uint8_t* blob, uint64_t size, uint32_t* H_out, uint32_t* S_out) {
+  if (!blob || size < 8) return false;
+  const int32_t S = rd_i32(blob), H = rd_i32(blob + 4);
+  if (S < 0 || S > VELO_MAX_MODULES || H < 0) return false;
+  if (size < 8ull + 12ull * (uint64_t)S + 16ull * (uint64_t)H) return false;
+  *H_out = (uint32_t)H;
+  *S_out = (uint32_t)S;
+  return true;
 }
 
 // Header and module-table checks (coordinates are checked on the device).
@@ -192,7 +262,7 @@ void sort_range(float* a, float* b, float* c, uint32_t* d, int lo, int hi) {
 }
 
 uint32_t resolve_threads(int32_t t) {
-  if (t == 64 || t == 128 || t == 256 || t == 512) return (uint32_t)t;
+  if (t == 32 || t == 64 || t == 128 || t == 256 || t == 512) return (uint32_t)t;
   return 256;
 }
 
@@ -285,6 +355,7 @@ velo_status velo_create(velo_ctx** out, int32_t device) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->l2_bytes, cudaDevAttrL2CacheSize, device);
   if (e == cudaSuccess) e = cudaEventCreate(&c->e0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->e1);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->meta_copied, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     velo_destroy(c);
     return VELO_ERR_CUDA;
@@ -310,6 +381,7 @@ void velo_destroy(velo_ctx* c) {
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
+  if (c->meta_copied) cudaEventDestroy(c->meta_copied);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -354,6 +426,7 @@ namespace {
 velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
                        int32_t n, bool direct) {
   if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  HostTimer timer(&c->stats.host_stage_ms);
   VELO_CUDA(c, cudaSetDevice(c->device));
   c->io_input = nullptr;
   c->staged = false;
@@ -361,11 +434,13 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   c->ran = false;
   c->generation++;
   c->n = n;
-  c->h_offset.assign(n, 0);
-  c->h_hits.assign(n, 0);
-  c->h_maxmod.assign(n, 0);
-  c->h_valid.assign(n, 0);
-  c->h_hit_base.assign(n, 0);
+  // the previous batch's metadata copies have left the pinned arrays
+  VELO_CUDA(c, cudaEventSynchronize(c->meta_copied));
+  if (!c->h_offset.assign(n, 0) || !c->h_hits.assign(n, 0) || !c->h_maxmod.assign(n, 0) ||
+      !c->h_valid.assign(n, 0) || !c->h_hit_base.assign(n, 0)) {
+    c->err = "pinned host metadata";
+    return VELO_ERR_OUT_OF_MEMORY;
+  }
   uint64_t lo = ~0ull, hi = 0;
   for (int32_t e = 0; e < n; ++e) {
     if (offsets[e] & 3u) {
@@ -381,12 +456,14 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
     return VELO_ERR_INVALID_ARGUMENT;
   }
   uint64_t rows = 0, hits = 0;
+  uint32_t max_modules = 0;
   for (int32_t e = 0; e < n; ++e) {
-    uint32_t H = 0, M = 0;
-    const bool ok = check_event(buf + offsets[e], sizes[e], &H, &M) == VELO_OK;
+    uint32_t H = 0, S = 0;
+    const bool ok = check_header(buf + offsets[e], sizes[e], &H, &S);
+    if (ok) max_modules = std::max(max_modules, S);
     c->h_valid[e] = ok ? 1u : 0u;
     c->h_hits[e] = ok ? H : 0u;
-    c->h_maxmod[e] = ok ? M : 0u;
+    c->h_maxmod[e] = 0u;   // the arena layout depends on H only
     c->h_offset[e] = offsets[e] - lo;
     c->h_hit_base[e] = rows;
     rows += std::max<uint64_t>(c->h_hits[e], 1ull);
@@ -394,6 +471,7 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   }
   c->rows = rows;
   c->total_hits = hits;
+  c->max_modules = max_modules;
   c->input_bytes = hi - lo;
   velo_status st;
   if (direct && hi > lo) c->io_input = static_cast<const uint8_t*>(device_view(buf + lo));
@@ -411,15 +489,17 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   if ((st = ensure(c, c->d_out_first, 8ull * n, "first")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_out_status, 4ull * n, "status")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_counters, 64, "counters")) != VELO_OK) return st;
-  if (hi > lo && !c->io_input)
-    VELO_CUDA(c, cudaMemcpyAsync(c->d_input.p, buf + lo, hi - lo, cudaMemcpyHostToDevice, c->stream));
   if (n > 0) {
     VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_offset.p, c->h_offset.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
     VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_hits.p, c->h_hits.data(), 4ull * n, cudaMemcpyHostToDevice, c->stream));
     VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_maxmod.p, c->h_maxmod.data(), 4ull * n, cudaMemcpyHostToDevice, c->stream));
     VELO_CUDA(c, cudaMemcpyAsync(c->d_ev_valid.p, c->h_valid.data(), 4ull * n, cudaMemcpyHostToDevice, c->stream));
     VELO_CUDA(c, cudaMemcpyAsync(c->d_hit_base.p, c->h_hit_base.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
+    VELO_CUDA(c, cudaEventRecord(c->meta_copied, c->stream));
   }
+  // the events last, so that waiting for the metadata copies never waits for them
+  if (hi > lo && !c->io_input)
+    VELO_CUDA(c, cudaMemcpyAsync(c->d_input.p, buf + lo, hi - lo, cudaMemcpyHostToDevice, c->stream));
   c->staged = true;
   return VELO_OK;
 }
@@ -462,7 +542,11 @@ velo_status prepare_launch(velo_ctx* c, const velo_options& o, uint32_t* smem_ou
   }
   const bool persistent = o.launch_mode == VELO_LAUNCH_PERSISTENT;
   if (!c->meta_valid || c->meta_smem != smem || c->meta_y != (int)Y || c->meta_persistent != (int)persistent) {
-    c->h_arena_off.assign(c->n, velo::kNoArena);
+    VELO_CUDA(c, cudaEventSynchronize(c->meta_copied));   // earlier copies have left the pinned arrays
+    if (!c->h_arena_off.assign(c->n, velo::kNoArena) || (persistent && !c->h_order.resize(c->n))) {
+      c->err = "pinned host metadata";
+      return VELO_ERR_OUT_OF_MEMORY;
+    }
     uint64_t goff = 0;
     int32_t nglob = 0;
     for (int32_t e = 0; e < c->n; ++e) {
@@ -481,15 +565,23 @@ velo_status prepare_launch(velo_ctx* c, const velo_options& o, uint32_t* smem_ou
       VELO_CUDA(c, cudaMemcpyAsync(c->d_arena_off.p, c->h_arena_off.data(), 8ull * c->n,
                                    cudaMemcpyHostToDevice, c->stream));
     if (persistent) {
-      c->h_order.resize(c->n);
-      std::iota(c->h_order.begin(), c->h_order.end(), 0);
-      std::stable_sort(c->h_order.begin(), c->h_order.end(),
-                       [&](int32_t a, int32_t b) { return c->h_hits[a] > c->h_hits[b]; });
+      // largest events first (load balance of the work queue): a counting
+      // sort on the hit count's top bits, stable within a bucket
+      constexpr int kBuckets = 1024;
+      uint32_t hmax = 1;
+      for (int32_t e = 0; e < c->n; ++e) hmax = std::max(hmax, c->h_hits[e]);
+      int shift = 0;
+      while ((hmax >> shift) >= (uint32_t)kBuckets) ++shift;
+      std::vector<int32_t> start(kBuckets + 1, 0);
+      for (int32_t e = 0; e < c->n; ++e) start[kBuckets - 1 - (int)(c->h_hits[e] >> shift) + 1]++;
+      for (int b = 0; b < kBuckets; ++b) start[b + 1] += start[b];
+      for (int32_t e = 0; e < c->n; ++e) c->h_order[start[kBuckets - 1 - (int)(c->h_hits[e] >> shift)]++] = e;
       if ((st = ensure(c, c->d_order, 4ull * c->n, "order")) != VELO_OK) return st;
       if (c->n > 0)
         VELO_CUDA(c, cudaMemcpyAsync(c->d_order.p, c->h_order.data(), 4ull * c->n,
                                      cudaMemcpyHostToDevice, c->stream));
     }
+    if (c->n > 0) VELO_CUDA(c, cudaEventRecord(c->meta_copied, c->stream));
     c->events_in_global = nglob;
     c->generation++;
     c->meta_valid = true;
@@ -544,6 +636,9 @@ int launch_mode_of(const velo_ctx* c, const velo_options& o) {
   return velo::kModePlain;
 }
 
+// Whether every staged event fits the compact shared-state build.
+bool compact_of(const velo_ctx* c) { return c->max_modules < (uint32_t)velo::kCompactModules; }
+
 // Dynamic shared memory of the launch: the arena, after the MLP weights when learned.
 uint32_t launch_smem(const velo_options& o, uint32_t arena_smem) {
   return arena_smem + (o.learned ? velo::kMlpSmemBytes : 0u);
@@ -558,7 +653,7 @@ velo_status launch_shape(velo_ctx* c, const velo_options& o, uint32_t smem, int*
     if (per_sm <= 0) {
       int occ = 0;
       int e = velo::search_occupancy(o.threads_per_event, launch_smem(o, smem), o.register_ctas,
-                                     launch_mode_of(c, o), &occ);
+                                     launch_mode_of(c, o), compact_of(c), &occ);
       if (e != 0) return cuda_fail(c, (cudaError_t)e, "occupancy");
       per_sm = std::max(occ, 1);
     }
@@ -610,7 +705,8 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
     p.dump_capacity = c->dump_capacity;
     p.dump_keep = c->dump_keep;
   }
-  int e = velo::launch_search(p, grid, o.threads_per_event, launch_smem(o, smem), c->stream, o.register_ctas);
+  int e = velo::launch_search(p, grid, o.threads_per_event, launch_smem(o, smem), c->stream, o.register_ctas,
+                              compact_of(c));
   if (e != 0) return cuda_fail(c, (cudaError_t)e, "search kernel launch");
   return VELO_OK;
 }
@@ -658,6 +754,7 @@ velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
 velo_status velo_run(velo_ctx* c, const velo_options* opts) {
   if (!c) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
+  HostTimer timer(&c->stats.host_launch_ms);
   velo_options o;
   velo_status st = check_options(c, opts, &o);
   if (st != VELO_OK) return st;
@@ -687,6 +784,7 @@ velo_status velo_fetch(velo_ctx* c, velo_track* tracks_out, uint64_t capacity, u
   if (!c->ran) return VELO_ERR_NOT_STAGED;
   VELO_CUDA(c, cudaSetDevice(c->device));
   VELO_CUDA(c, cudaStreamSynchronize(c->stream));
+  HostTimer timer(&c->stats.host_fetch_ms);
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, c->e0, c->e1) == cudaSuccess) c->stats.kernel_ms = ms;
   unsigned long long total = 0;
@@ -792,7 +890,7 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
   const int32_t part = o.pipeline_events;
   const int32_t n_parts = (n + part - 1) / part;
   uint64_t base = 0, hits = 0, in_bytes = 0;
-  float kernel_ms = 0.f;
+  float kernel_ms = 0.f, stage_ms = 0.f, launch_ms = 0.f, fetch_ms = 0.f;
   int32_t bad_event = -1;
   velo_status first_error = VELO_OK;
   auto finish = [&](int32_t k) -> velo_status {
@@ -815,6 +913,9 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
     hits += ch->stats.total_hits;
     in_bytes += ch->stats.input_bytes;
     kernel_ms += ch->stats.kernel_ms;
+    stage_ms += ch->stats.host_stage_ms;
+    launch_ms += ch->stats.host_launch_ms;
+    fetch_ms += ch->stats.host_fetch_ms;
     return VELO_OK;
   };
   for (int32_t k = 0; k < n_parts; ++k) {
@@ -865,6 +966,9 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
   c->stats.total_tracks = base;
   c->stats.output_bytes = 4ull * n + sizeof(velo_track) * base;
   c->stats.kernel_ms = kernel_ms;
+  c->stats.host_stage_ms = stage_ms;
+  c->stats.host_launch_ms = launch_ms;
+  c->stats.host_fetch_ms = fetch_ms;
   c->stats.launches = (uint32_t)n_parts;
   if (bad_event >= 0) {
     c->err = "event " + std::to_string(bad_event) + " failed validation";
@@ -1015,8 +1119,9 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
   // threads per event x shared-memory tile (hits staged per CTA; 0 = the
   // automatic budget) x register build x launch style; narrowing stays on
   // (it only removes work) and y_lanes is the caller's (it defines results)
+  // (32-thread CTAs are supported but measured far slower: 1.5x at best)
   static const int32_t kThreads[] = {64, 128, 256, 512};
-  static const int32_t kSmemHits[] = {0, 300, 600, 900, 1200, 1600, 2400};
+  static const int32_t kSmemHits[] = {0, 50, 100, 200, 300, 600, 900, 1200, 1600, 2400};
   static const int32_t kRegs[] = {4, 5};
   static const int32_t kModes[] = {VELO_LAUNCH_PER_EVENT, VELO_LAUNCH_PERSISTENT};
   float best = 0.f;

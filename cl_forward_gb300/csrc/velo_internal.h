@@ -29,6 +29,9 @@ constexpr int kMaxModuleHits = VELO_MAX_MODULE_HITS;
 constexpr uint32_t kTrackletFlag = 0x80000000u;
 constexpr uint32_t kSkipMask = 0x70000000u;
 constexpr uint64_t kNoArena = ~0ull;
+// Module-table capacity of the compact shared-state build of the search
+// kernel (events with fewer modules; the full build takes kMaxModules).
+constexpr int kCompactModules = 64;
 
 // MLP parameter layout (velo_search.h): W1[32][10] b1[32] W2[32][32] b2[32]
 // W3[2][32] b3[2]
@@ -131,11 +134,14 @@ struct SearchParams {
 
 // Launches the search kernel (velo_kernels.cu); reg_ctas (4 or 5) picks the
 // register budget of the <= 256-thread build.  Returns a cudaError_t value.
-int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas);
+// compact: every event of the launch has fewer than 64 modules (the compact
+// shared-state build).
+int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas,
+                  bool compact);
 // Sets the kernels' maximum dynamic shared memory.  Returns a cudaError_t value.
 int configure_search_kernel(uint32_t smem_bytes);
 // Maximum resident CTAs per SM for a block size, shared-memory size and build.
-int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, int* ctas_per_sm);
+int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, bool compact, int* ctas_per_sm);
 // Straight-line fits of the compacted output tracks (velo_fit.cu).
 int launch_fit_tracks(const uint8_t* input, const uint64_t* ev_offset, const uint32_t* ev_valid,
                       const velo_track* tracks, const uint32_t* counts, const uint64_t* first, int n_events,

@@ -51,13 +51,18 @@ __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b)
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kNone16 = 0xffffu;
 
-struct Shared {
-  int32_t start[kMaxModules + 1];
-  int32_t num[kMaxModules + 1];
-  int32_t sz[kMaxModules + 1];
-  float zmin[kMaxModules + 1];
-  float zmax[kMaxModules + 1];
-  uint8_t sorted[kMaxModules + 1];
+// Per-CTA shared state for events of up to kMods modules.  Launches whose
+// events all have at most kCompactModules - 1 modules (every VELO geometry)
+// use the compact form: 4 KB less static shared memory per CTA, which goes
+// to L1 and to more resident CTAs.
+template <int kMods>
+struct SharedT {
+  int32_t start[kMods];
+  int32_t num[kMods];
+  int32_t sz[kMods];
+  float zmin[kMods];
+  float zmax[kMods];
+  uint8_t sorted[kMods];
   uint32_t ring_lo[2];   // forwarding entries, from the front of ring[i]
   uint32_t ring_hi[2];   // seeding entries, from the back of ring[i]
   uint32_t ntracks, ntracklets, nweak, status;
@@ -123,6 +128,7 @@ __device__ __forceinline__ void narrow_range(const float* x, int lo0, int hi0, f
 // ---------------------------------------------------------------------------
 // Candidate windows of hit h on module f (Kernel.cl:50-178), stored relative
 // to the start of module f-2 (0xffff = none).
+template <class Shared>
 __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int f) {
   const int s2 = f - 2;
   const bool proc_h2 = f <= ev.S - 3;
@@ -217,6 +223,7 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, bool take) {
 // (a select, not an indexed array, so the view stays in registers)
 __device__ __forceinline__ uint32_t* ring_buf(const EventView& ev, int b) { return b ? ev.ring1 : ev.ring0; }
 
+template <class Shared>
 __device__ __forceinline__ void push_back(Shared& s, const EventView& ev, int b, uint32_t v) {
   const uint32_t i = atomicAdd(&s.ring_hi[b], 1u);
   if (i < ev.ring_cap) ring_buf(ev, b)[ev.ring_cap - 1u - i] = v;
@@ -232,6 +239,7 @@ __device__ __forceinline__ uint32_t ring_entry(const EventView& ev, int b, uint3
 // lane j forwards entry i0 + j of ring[b].  Track numbers, ring slots and
 // weak slots are reserved with one atomic per warp; new entries go to the
 // front of ring[nb].
+template <class Shared>
 __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_n, uint32_t i0, uint32_t ncur,
                              int m4, int nb) {
   enum { kNone = 0, kPushTrack, kNewTrack, kPushSkip, kWeak };
@@ -376,7 +384,7 @@ constexpr int kLearned = 2;  // MLP-pruned seeding
 // with the unused-h0 gather of :720-764).  One warp per h0; lane j of chunk c
 // takes h1 element e = 32c + j, which belongs to the reference's Y-lane
 // e mod Y.  New tracklets go to the back of ring[nb].
-template <int kMode>
+template <int kMode, class Shared>
 __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint32_t below_same_lane,
                             uint32_t lane_mod) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -558,7 +566,7 @@ __device__ unsigned long long g_phase_cycles[8];
 #endif
 
 // ---------------------------------------------------------------------------
-template <int kMode>
+template <int kMode, class Shared>
 __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* dyn, const MlpFrag* mlp_smem) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
@@ -610,13 +618,18 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   ev.dump_capacity = p.dump_capacity;
   ev.dump_keep = p.dump_keep > 0 ? p.dump_keep : 1u;
 
-  // stage the event
+  // stage the event; the module table must tile [0, H) in order (the host
+  // checked only the header and the blob's length)
+  bool bad = tid == 0 && S == 0 && H != 0;
   for (int m = tid; m < S; m += nt) {
-    s.start[m] = gstart[m];
-    s.num[m] = gnum[m];
+    const int32_t st = gstart[m], nm = gnum[m];
+    const int64_t expect = m == 0 ? 0 : (int64_t)gstart[m - 1] + (int64_t)gnum[m - 1];
+    bad |= nm < 0 || nm > VELO_MAX_MODULE_HITS || (int64_t)st != expect ||
+           (m == S - 1 && (int64_t)st + (int64_t)nm != (int64_t)H);
+    s.start[m] = st;
+    s.num[m] = nm;
     s.sz[m] = gZ[m];
   }
-  bool bad = false;
   for (int i = tid; i < H; i += nt) {
     const float xv = gx[i], yv = gy[i], zv = gz[i];
     bad |= !(isfinite(xv) && isfinite(yv) && isfinite(zv));
@@ -630,7 +643,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
     s.considered = 0; s.kept = 0;
   }
-  if (__syncthreads_or(bad)) {   // coordinates must be finite (the host checks only the tables)
+  if (__syncthreads_or(bad)) {   // a bad module table, or a non-finite coordinate
     if (tid == 0) {
       p.out_counts[e] = 0;
       p.out_first[e] = 0;
@@ -794,10 +807,10 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
 // Three instantiations: up to 256 threads per CTA with registers budgeted
 // for 4 or for 5 resident CTAs per SM (velo_options.register_ctas), and
 // 512-thread CTAs.
-template <int kMaxThreads, int kMinCtas, int kMode>
+template <int kMaxThreads, int kMinCtas, int kMode, int kMods>
 __global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const SearchParams p) {
   extern __shared__ __align__(16) uint8_t dyn_smem_raw[];
-  __shared__ Shared s;
+  __shared__ SharedT<kMods> s;
   // learned seeding: the MLP weights lead the dynamic shared memory
   const MlpFrag* mlp_smem = nullptr;
   uint8_t* dyn_smem = dyn_smem_raw;
@@ -822,13 +835,17 @@ __global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const Sea
   }
 }
 
-#define VELO_KERNEL_R4 search_kernel<256, 4, kPlain>
-#define VELO_KERNEL_R5 search_kernel<256, 5, kPlain>
-#define VELO_KERNEL_LARGE search_kernel<512, 1, kPlain>
-#define VELO_KERNEL_DUMP search_kernel<256, 4, kDump>
-#define VELO_KERNEL_LEARNED search_kernel<256, 4, kLearned>
+constexpr int kFullModules = kMaxModules + 1;
+#define VELO_KERNEL_R4 search_kernel<256, 4, kPlain, kFullModules>
+#define VELO_KERNEL_R5 search_kernel<256, 5, kPlain, kFullModules>
+#define VELO_KERNEL_R4C search_kernel<256, 4, kPlain, kCompactModules>
+#define VELO_KERNEL_R5C search_kernel<256, 5, kPlain, kCompactModules>
+#define VELO_KERNEL_LARGE search_kernel<512, 1, kPlain, kFullModules>
+#define VELO_KERNEL_DUMP search_kernel<256, 4, kDump, kFullModules>
+#define VELO_KERNEL_LEARNED search_kernel<256, 4, kLearned, kFullModules>
 
-int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas) {
+int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas,
+                  bool compact) {
   cudaStream_t st = (cudaStream_t)stream;
   if (p.mlp)
     VELO_KERNEL_LEARNED<<<grid, min(block, 256), smem_bytes, st>>>(p);
@@ -836,8 +853,12 @@ int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_byte
     VELO_KERNEL_DUMP<<<grid, min(block, 256), smem_bytes, st>>>(p);
   else if (block > 256)
     VELO_KERNEL_LARGE<<<grid, block, smem_bytes, st>>>(p);
+  else if (reg_ctas == 4 && compact)
+    VELO_KERNEL_R4C<<<grid, block, smem_bytes, st>>>(p);
   else if (reg_ctas == 4)
     VELO_KERNEL_R4<<<grid, block, smem_bytes, st>>>(p);
+  else if (compact)
+    VELO_KERNEL_R5C<<<grid, block, smem_bytes, st>>>(p);
   else
     VELO_KERNEL_R5<<<grid, block, smem_bytes, st>>>(p);
   return (int)cudaGetLastError();
@@ -855,6 +876,10 @@ int configure_search_kernel(uint32_t smem_bytes) {
   e = cudaFuncSetAttribute(VELO_KERNEL_R4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(VELO_KERNEL_R5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_R4C, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_R5C, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(VELO_KERNEL_LARGE, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
@@ -875,7 +900,7 @@ extern "C" int velo_debug_phase_cycles(unsigned long long* out) {
 }
 #endif
 
-int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, int* ctas_per_sm) {
+int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, bool compact, int* ctas_per_sm) {
   if (mode == kLearned)
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_LEARNED, min(block, 256),
                                                               smem_bytes);
@@ -885,8 +910,10 @@ int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, int
   if (block > 256)
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_LARGE, block, smem_bytes);
   if (reg_ctas == 4)
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_R4, block, smem_bytes);
-  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_R5, block, smem_bytes);
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, compact ? VELO_KERNEL_R4C : VELO_KERNEL_R4,
+                                                              block, smem_bytes);
+  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, compact ? VELO_KERNEL_R5C : VELO_KERNEL_R5,
+                                                            block, smem_bytes);
 }
 
 }  // namespace velo

@@ -46,6 +46,14 @@ __global__ void sort_modules_kernel(uint8_t* input, const uint64_t* offsets, con
   float* x = reinterpret_cast<float*>(id + H);
   float* y = x + H;
   float* z = y + H;
+  // the module table must tile [0, H) in order before anything moves
+  bool bad = threadIdx.x == 0 && S == 0 && H != 0;
+  for (int m = threadIdx.x; m < S; m += blockDim.x) {
+    const int64_t expect = m == 0 ? 0 : (int64_t)start[m - 1] + (int64_t)num[m - 1];
+    bad |= num[m] < 0 || num[m] > VELO_MAX_MODULE_HITS || (int64_t)start[m] != expect ||
+           (m == S - 1 && (int64_t)start[m] + (int64_t)num[m] != (int64_t)H);
+  }
+  if (__syncthreads_or(bad)) return;
   for (int m = threadIdx.x; m < S; m += blockDim.x) {
     // a non-finite x would stall the partition (the reference's sort never
     // returns on a NaN); such a module stays unsorted and the search marks

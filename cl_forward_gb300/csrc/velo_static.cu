@@ -213,6 +213,6 @@ extern "C" velo_status velo_search_device_static(const uint8_t* d_input, const u
   p.out_status = d_status;
   p.out_cursor = v.cursor;
   p.work_counter = v.work;
-  if (launch_search(p, n_events, 256, smem, s, 5) != 0) return VELO_ERR_CUDA;
+  if (launch_search(p, n_events, 256, smem, s, 5, false) != 0) return VELO_ERR_CUDA;
   return VELO_OK;
 }

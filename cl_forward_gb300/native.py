@@ -76,7 +76,8 @@ class Stats(ctypes.Structure):
                 ("total_tracks", ctypes.c_uint64), ("input_bytes", ctypes.c_uint64),
                 ("output_bytes", ctypes.c_uint64), ("smem_bytes_per_cta", ctypes.c_int32),
                 ("grid", ctypes.c_int32), ("block", ctypes.c_int32),
-                ("events_in_global", ctypes.c_int32)]
+                ("events_in_global", ctypes.c_int32), ("host_stage_ms", ctypes.c_float),
+                ("host_launch_ms", ctypes.c_float), ("host_fetch_ms", ctypes.c_float)]
 
 
 class VeloError(RuntimeError):

@@ -81,7 +81,7 @@ typedef enum velo_launch_mode {
 
 typedef struct velo_options {
   int32_t y_lanes;            /* reference local size dim 1 (1..16); its output uses 4 */
-  int32_t threads_per_event;  /* 64, 128, 256 or 512 */
+  int32_t threads_per_event;  /* 32, 64, 128, 256 or 512 */
   int32_t launch_mode;        /* velo_launch_mode */
   int32_t smem_hits;          /* largest event (hits) staged in shared memory; 0 = auto */
   int32_t narrow_windows;     /* 1: binary-search narrowing of x windows (decisions unchanged) */
@@ -116,6 +116,9 @@ typedef struct velo_stats {
   int32_t grid;
   int32_t block;
   int32_t events_in_global;   /* events too large for the shared-memory arena */
+  float host_stage_ms;        /* host time of the last stage: checks, metadata, enqueueing copies */
+  float host_launch_ms;       /* host time of the last velo_run: launch preparation and enqueueing */
+  float host_fetch_ms;        /* host time of the last fetch after the search finished: result copies */
 } velo_stats;
 
 typedef struct velo_ctx velo_ctx;

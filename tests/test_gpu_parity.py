@@ -67,7 +67,7 @@ def test_fuzz_ties_and_lanes(gpu_ctx, oracle_lib, y):
     assert n > 200
 
 
-@pytest.mark.parametrize("threads", [64, 128, 256, 512])
+@pytest.mark.parametrize("threads", [32, 64, 128, 256, 512])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_launch_shapes(gpu_ctx, oracle_lib, threads, mode):
     from cl_forward_gb300 import generator
@@ -163,10 +163,27 @@ def test_edge_cases(gpu_ctx, oracle_lib):
     ev = events.unpack_event(good[1])
     ev.y[5] = np.inf
     nonfinite = events.pack_event(ev)
-    batch = [good[0], fuzz.empty_event(), nonfinite, b"\x05\x00\x00\x00", fuzz.empty_event(0), good[2]]
+    # module tables that do not tile [0, H): checked on the device
+    raw = np.frombuffer(good[1], np.int32).copy()
+    S = int(raw[0])
+    gap = raw.copy()
+    gap[2 + 2 * S + 7] -= 1                                # module 7 one hit short: starts stop lining up
+    over = raw.copy()
+    over[2 + 2 * S + S - 1] += 1                           # last module runs past H
+    batch = [good[0], fuzz.empty_event(), nonfinite, b"\x05\x00\x00\x00", fuzz.empty_event(0), good[2],
+             gap.tobytes(), over.tobytes()]
     got, status = gpu_ctx.search(batch, allow_invalid=True)
     assert status[2] & native.EVENT_INVALID and status[3] & native.EVENT_INVALID
+    assert status[6] & native.EVENT_INVALID and status[7] & native.EVENT_INVALID
     assert len(got[1]) == 0 and len(got[2]) == 0 and len(got[3]) == 0 and len(got[4]) == 0
+    assert len(got[6]) == 0 and len(got[7]) == 0
+    pbuf, poffs, psizes = events.pack_events(batch)
+    gpu_ctx.stage(pbuf, poffs, psizes)
+    gpu_ctx.sort_staged()
+    staged = gpu_ctx.fetch_staged(len(pbuf))
+    for k in (6, 7):                                          # the device sort leaves them alone
+        a, n = int(poffs[k]), int(psizes[k])
+        assert bytes(staged[a:a + n]) == batch[k]
     want, _ = oracle_lib.search([good[0], good[2]], 4)
     assert index_lists(got[0]) == index_lists(want[0])
     assert index_lists(got[5]) == index_lists(want[1])
