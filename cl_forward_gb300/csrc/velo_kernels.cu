@@ -112,6 +112,13 @@ __device__ __forceinline__ void narrow_range(const float* x, int lo0, int hi0, f
   const float lt = fsub(fsub(xl, tol), margin);
   const float ht = fadd(fadd(xh, tol), margin);
   if (isfinite(lt) && isfinite(ht)) {
+    // both ends first (two independent loads): a prediction beyond either end
+    // of the module (a track tried on the other detector half) is settled
+    // without the bisection, with the bisection's own result
+    if (lo0 < hi0 && (x[hi0 - 1] <= lt || x[lo0] > ht)) {
+      *lo = *hi = x[lo0] > ht ? lo0 : hi0;
+      return;
+    }
     const int l = first_gt(x, lo0, hi0, lt);
     int h = l;
     const int walk_end = min(hi0, l + 8);
@@ -357,23 +364,36 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
 // Features of an (h0, h1) doublet seen by the learned seeding (and recorded
 // as training data): slopes, h0 radius and azimuth, module, predicted x / y
 // at module f-4, z gap, h2 candidates in the exact window, and the y-slope
-// cut margin.  Plain FP32; the features steer pruning, not the cuts.
-__device__ __forceinline__ void doublet_features(float* f, float h0x, float h0y, float h0z, float h1x, float h1y,
-                                                 float h1z, int module, int n_modules, float zmid4, int h2_window,
-                                                 float dymax) {
-  const float dz = h1z - h0z;
-  const float inv = 1.f / dz;
-  const float tx = (h1x - h0x) * inv, ty = (h1y - h0y) * inv;
+// cut margin.  Plain FP32; the features steer pruning, not the cuts.  The
+// h0 terms (radius, azimuth, module, 1 / dymax) are computed once per h0 by
+// h0_features; dz_inv is the seeding's own 1 / (z1 - z0).
+struct H0Features {
+  float r, phi, module, inv_dymax;
+};
+
+__device__ __forceinline__ H0Features h0_features(float h0x, float h0y, int module, int n_modules, float dymax) {
+  H0Features g;
+  g.r = sqrtf(h0x * h0x + h0y * h0y) * (1.f / 42.f);
+  g.phi = atan2f(h0y, h0x) * 0.31830988f;
+  g.module = (float)module / (float)n_modules;
+  g.inv_dymax = 1.f / dymax;
+  return g;
+}
+
+__device__ __forceinline__ void doublet_features(float* f, const H0Features& g, float h0x, float h0y, float h0z,
+                                                 float h1x, float h1y, float h1z, float dz_inv, float zmid4,
+                                                 int h2_window) {
+  const float tx = (h1x - h0x) * dz_inv, ty = (h1y - h0y) * dz_inv;
   f[0] = 5.f * tx;
   f[1] = 5.f * ty;
-  f[2] = sqrtf(h0x * h0x + h0y * h0y) * (1.f / 42.f);
-  f[3] = atan2f(h0y, h0x) * 0.31830988f;
-  f[4] = (float)module / (float)n_modules;
+  f[2] = g.r;
+  f[3] = g.phi;
+  f[4] = g.module;
   f[5] = (h0x + tx * (zmid4 - h0z)) * (1.f / 42.f);
   f[6] = (h0y + ty * (zmid4 - h0z)) * (1.f / 42.f);
-  f[7] = dz * 0.01f;
+  f[7] = (h1z - h0z) * 0.01f;
   f[8] = (float)h2_window * (1.f / 32.f);
-  f[9] = fabsf(h1y - h0y) / dymax;
+  f[9] = fabsf(h1y - h0y) * g.inv_dymax;
 }
 
 constexpr int kPlain = 0;    // the reference's seeding
@@ -400,6 +420,10 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
   const float* y4 = ev.y + st4;
   const float* z4 = ev.z + st4;
   bool degenerate = false;
+  // 1 / (z1 - z0) by bit patterns of (z0, z1): hits of a module share few z
+  // values, so the division is rarely redone (same operands, same result)
+  uint32_t zk0 = 0x7fc00001u, zk1 = 0x7fc00001u;
+  float dz_inv_cached = 0.f;
 
   for (int i = warp; i < n0; i += nwarps) {
     const int h0 = st0 + i;
@@ -410,6 +434,8 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
     const int n1 = (int)(w0 >> 16) - (int)f1;        // > 0 when a first hit was found
     const float h0x = ev.x[h0], h0y = ev.y[h0], h0z = ev.z[h0];
     const float dymax = fmul(kMaxYSlope, fabsf(fsub(s1_z, h0z)));
+    H0Features g0{};
+    if constexpr (kMode != kPlain) g0 = h0_features(h0x, h0y, f, ev.S, dymax);
     unsigned long long best = ~0ull;
     uint32_t dead_lanes = 0;                         // Y-lanes already stopped (bit per lane)
     uint32_t chunk_mod = 0;
@@ -437,11 +463,20 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
       }
       int a = (int)(w1 & 0xffffu), b = (int)(w1 >> 16);
       float tol = kTolerance;
+      float dz_inverted = 0.f;
+      if (cand) {
+        if (__float_as_uint(h1z) != zk1 || __float_as_uint(h0z) != zk0) {
+          zk0 = __float_as_uint(h0z);
+          zk1 = __float_as_uint(h1z);
+          dz_inv_cached = fdiv(1.f, fsub(h1z, h0z));
+        }
+        dz_inverted = dz_inv_cached;
+      }
       if constexpr (kMode != kPlain) {
         bool keep = cand;
         float feat[kMlpIn];
         if (cand) {
-          doublet_features(feat, h0x, h0y, h0z, h1x, h1y, h1z, f, ev.S, 0.5f * (zmin4 + zmax4), b - a, dymax);
+          doublet_features(feat, g0, h0x, h0y, h0z, h1x, h1y, h1z, dz_inverted, 0.5f * (zmin4 + zmax4), b - a);
           if constexpr (kMode == kDump) {
             uint32_t hs = (uint32_t)ev.event * 0x9E3779B1u ^ (uint32_t)h0 * 0x85EBCA77u ^ (uint32_t)h1 * 0xC2B2AE3Du;
             hs ^= hs >> 15;
@@ -480,7 +515,6 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
         }
       }
       if (!cand) continue;
-      const float dz_inverted = fdiv(1.f, fsub(h1z, h0z));
       const float ddx = fsub(h1x, h0x), ddy = fsub(h1y, h0y);
       if (narrow4) {
         const float xa = fadd(h0x, fmul(ddx, fmul(fsub(zmin4, h0z), dz_inverted)));
@@ -843,11 +877,14 @@ constexpr int kFullModules = kMaxModules + 1;
 #define VELO_KERNEL_LARGE search_kernel<512, 1, kPlain, kFullModules>
 #define VELO_KERNEL_DUMP search_kernel<256, 4, kDump, kFullModules>
 #define VELO_KERNEL_LEARNED search_kernel<256, 4, kLearned, kFullModules>
+#define VELO_KERNEL_LEARNED_C search_kernel<256, 4, kLearned, kCompactModules>
 
 int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas,
                   bool compact) {
   cudaStream_t st = (cudaStream_t)stream;
-  if (p.mlp)
+  if (p.mlp && compact)
+    VELO_KERNEL_LEARNED_C<<<grid, min(block, 256), smem_bytes, st>>>(p);
+  else if (p.mlp)
     VELO_KERNEL_LEARNED<<<grid, min(block, 256), smem_bytes, st>>>(p);
   else if (p.dump_features)
     VELO_KERNEL_DUMP<<<grid, min(block, 256), smem_bytes, st>>>(p);
@@ -886,6 +923,8 @@ int configure_search_kernel(uint32_t smem_bytes) {
     e = cudaFuncSetAttribute(VELO_KERNEL_DUMP, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(VELO_KERNEL_LEARNED, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_LEARNED_C, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess && dev >= 0 && dev < 64) configured[dev] = smem_bytes;
   return (int)e;
 }
@@ -902,8 +941,8 @@ extern "C" int velo_debug_phase_cycles(unsigned long long* out) {
 
 int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, bool compact, int* ctas_per_sm) {
   if (mode == kLearned)
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_LEARNED, min(block, 256),
-                                                              smem_bytes);
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        ctas_per_sm, compact ? VELO_KERNEL_LEARNED_C : VELO_KERNEL_LEARNED, min(block, 256), smem_bytes);
   if (mode == kDump)
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_DUMP, min(block, 256),
                                                               smem_bytes);

@@ -287,7 +287,7 @@ def main(argv=None):
     w0 = init_weights(0)
     thr0, _ = calibrate(w0, cal, recall=a.recall)
     kept0 = keep_fraction(w0, cal, thr0)
-    base = native.default_options(launch_mode=1, threads_per_event=128, smem_hits=600, register_ctas=4)
+    base = native.default_options(launch_mode=1, threads_per_event=64, smem_hits=50, register_ctas=4)
     res4 = compare_paths(ctx, held_blobs, held_truths, w, thr, margin, a.min_keep_rate, base, max_hits=max_hits)
     report = {"config4": {"train_events": len(train_blobs), "train_doublets": int(len(ds.x)),
                           "train_positive": int(ds.label.sum()), "steps": a.steps, "batch": 4096, "lr": 1e-3,
