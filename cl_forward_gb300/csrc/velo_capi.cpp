@@ -80,7 +80,7 @@ struct velo_ctx {
   std::string err;
 
   DevBuf d_input, d_ev_offset, d_ev_hits, d_ev_maxmod, d_ev_valid, d_hit_base, d_arena_off, d_order;
-  DevBuf d_tracklets, d_weak, d_tracks, d_out_tracks, d_out_counts, d_out_first, d_out_status;
+  DevBuf d_tracklets, d_rings, d_weak, d_tracks, d_out_tracks, d_out_counts, d_out_first, d_out_status;
   DevBuf d_counters, d_garena, d_flush, d_fits;
 
   // staged batch
@@ -371,7 +371,7 @@ void velo_destroy(velo_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   DevBuf* bufs[] = {&c->d_input, &c->d_ev_offset, &c->d_ev_hits, &c->d_ev_maxmod, &c->d_ev_valid,
-                    &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_weak,
+                    &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_rings, &c->d_weak,
                     &c->d_tracks, &c->d_out_tracks, &c->d_out_counts, &c->d_out_first,
                     &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush, &c->d_mlp,
                     &c->d_dump_features, &c->d_dump_ids, &c->d_fits};
@@ -482,6 +482,7 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   if ((st = ensure(c, c->d_ev_valid, 4ull * n, "valid")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_hit_base, 8ull * n, "hit_base")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_tracklets, 16ull * rows, "tracklets")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_rings, 32ull * rows, "rings")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_weak, 4ull * rows, "weak")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_tracks, sizeof(velo_track) * rows, "tracks")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_out_tracks, sizeof(velo_track) * rows, "out_tracks")) != VELO_OK) return st;
@@ -682,6 +683,7 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
   p.smem_arena_bytes = smem;
   p.global_arena = P<uint8_t>(c->d_garena);
   p.tracklets = P<uint32_t>(c->d_tracklets);
+  p.rings = P<uint32_t>(c->d_rings);
   p.weak = P<uint32_t>(c->d_weak);
   p.tracks = P<velo_track>(c->d_tracks);
   p.out_tracks = c->io_tracks ? c->io_tracks : P<velo_track>(c->d_out_tracks);

@@ -61,12 +61,12 @@ constexpr uint32_t kMlpSmemBytes = (sizeof(MlpFrag) + 15) & ~15u;
 
 // Per-event working set ("arena"): staged in dynamic shared memory when it
 // fits the launch's shared-memory size, else carved from global scratch.
-// Offsets are bytes, each array 16-byte aligned.  29 bytes per hit.
+// Offsets are bytes, each array 16-byte aligned.  21 bytes per hit.  (The
+// tracks-to-follow rings live with the per-row scratch in global memory.)
 struct ArenaLayout {
   uint32_t x, y, z;              // float[H]    hit coordinates (x-sorted per module)
   uint32_t win;                  // uint2[H]    candidate windows, 16-bit offsets into module f-2
   uint32_t used;                 // uint8[H]    hit_used
-  uint32_t ring0, ring1;         // uint32[H+1] tracks-to-follow, double-buffered
   uint32_t total;
 };
 
@@ -84,8 +84,6 @@ VELO_HD ArenaLayout arena_layout(uint32_t H, uint32_t M, uint32_t Y) {
   L.z = o; o = align16(o + 4u * H);
   L.win = o; o = align16(o + 8u * H);
   L.used = o; o = align16(o + H);
-  L.ring0 = o; o = align16(o + 4u * (H + 1u));
-  L.ring1 = o; o = align16(o + 4u * (H + 1u));
   L.total = o;
   return L;
 }
@@ -109,6 +107,9 @@ struct SearchParams {
   // global scratch
   uint8_t* global_arena;
   uint32_t* tracklets;            // 4 words per tracklet {h0, h1, h2, 0}, row hit_base[e]
+  uint32_t* rings;                // 8 words per row: the two tracks-to-follow rings of event e
+                                  // (max(H, 1) entries each) from row hit_base[e], entries
+                                  // {entry word, first hit, previous hit, last hit}
   uint32_t* weak;                 // weak-track list, row hit_base[e]
   velo_track* tracks;             // working tracks, row hit_base[e]
   // outputs

@@ -74,12 +74,12 @@ struct SharedT {
 struct EventView {
   int S, H, Y;
   uint32_t cap;             // tracklet / track / weak rows (max(H, 1))
-  uint32_t ring_cap;        // entries of each tracks-to-follow buffer (H + 1)
+  uint32_t ring_cap;        // entries of each tracks-to-follow buffer (max(H, 1): one per seeded h0 at most)
   float *x, *y, *z;
   uint2* win;               // per hit: {h1 first | h1 last << 16, h2 first | h2 last << 16}
   uint8_t* used;
-  uint32_t* ring0;          // tracks-to-follow buffers, selected by parity
-  uint32_t* ring1;
+  uint4* ring0;             // tracks-to-follow buffers, selected by parity:
+  uint4* ring1;             //   {entry word, first hit, previous hit, last hit}
   uint4* tracklets;         // {h0, h1, h2, 0} per tracklet
   uint32_t* weak;
   velo_track* tracks;
@@ -228,17 +228,19 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, bool take) {
 }
 
 // (a select, not an indexed array, so the view stays in registers)
-__device__ __forceinline__ uint32_t* ring_buf(const EventView& ev, int b) { return b ? ev.ring1 : ev.ring0; }
+__device__ __forceinline__ uint4* ring_buf(const EventView& ev, int b) { return b ? ev.ring1 : ev.ring0; }
 
+// A ring entry carries the track's last two hits (and a tracklet's first), so
+// forwarding extrapolates without reading the track or tracklet row first.
 template <class Shared>
-__device__ __forceinline__ void push_back(Shared& s, const EventView& ev, int b, uint32_t v) {
+__device__ __forceinline__ void push_back(Shared& s, const EventView& ev, int b, uint4 v) {
   const uint32_t i = atomicAdd(&s.ring_hi[b], 1u);
   if (i < ev.ring_cap) ring_buf(ev, b)[ev.ring_cap - 1u - i] = v;
 }
 
 // i-th entry of ring[b]: the front segment, then the back segment.
-__device__ __forceinline__ uint32_t ring_entry(const EventView& ev, int b, uint32_t lo, uint32_t i) {
-  const uint32_t* r = ring_buf(ev, b);
+__device__ __forceinline__ uint4 ring_entry(const EventView& ev, int b, uint32_t lo, uint32_t i) {
+  const uint4* r = ring_buf(ev, b);
   return i < lo ? r[i] : r[ev.ring_cap - 1u - (i - lo)];
 }
 
@@ -253,24 +255,15 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
   const uint32_t i = i0 + (threadIdx.x & 31);
   int action = kNone;
   uint32_t push_value = 0, trackno = 0, best_h2 = 0;
-  uint4 tl = make_uint4(0, 0, 0, 0);
+  uint4 en = make_uint4(0, 0, 0, 0);
   if (i < ncur) {
-    const uint32_t full = ring_entry(ev, b, lo_n, i);
+    en = ring_entry(ev, b, lo_n, i);
+    const uint32_t full = en.x;
     const bool is_tracklet = (full & kTrackletFlag) != 0;
     const uint32_t skipped = (full & kSkipMask) >> 28;
     trackno = full & kEntryNumber;
-    uint32_t n, h0, h1;
-    if (is_tracklet) {
-      tl = ev.tracklets[trackno];
-      n = 3;
-      h0 = tl.y;
-      h1 = tl.z;
-    } else {
-      n = (full >> kEntryCountShift) & 31u;
-      const velo_track& t = ev.tracks[trackno];
-      h0 = t.hits[n - 2];
-      h1 = t.hits[n - 1];
-    }
+    const uint32_t n = is_tracklet ? 3u : (full >> kEntryCountShift) & 31u;
+    const uint32_t h0 = en.z, h1 = en.w;   // the last two hits
     const float h0x = ev.x[h0], h0y = ev.y[h0], h0z = ev.z[h0];
     const float h1x = ev.x[h1], h1y = ev.y[h1], h1z = ev.z[h1];
     const float td = fdiv(1.0f, fsub(h1z, h0z));
@@ -320,9 +313,9 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
       } else {
         ev.used[best_h2] = 1;
         if (is_tracklet) {   // third -> fourth hit: a track is allocated below; hits 0-2 marked
-          ev.used[tl.x] = 1;
-          ev.used[tl.y] = 1;
-          ev.used[tl.z] = 1;
+          ev.used[en.y] = 1;
+          ev.used[en.z] = 1;
+          ev.used[en.w] = 1;
           action = kNewTrack;
         } else {
           velo_track& t = ev.tracks[trackno];
@@ -344,7 +337,7 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
   if (action == kNewTrack) {
     if (tn < ev.cap) {
       uint32_t* w = reinterpret_cast<uint32_t*>(&ev.tracks[tn]);
-      w[0] = 4; w[1] = tl.x; w[2] = tl.y; w[3] = tl.z; w[4] = best_h2;
+      w[0] = 4; w[1] = en.y; w[2] = en.z; w[3] = en.w; w[4] = best_h2;
 #pragma unroll
       for (int k = 5; k < 25; ++k) w[k] = 0;
       push_value = tn | (4u << kEntryCountShift);
@@ -355,7 +348,9 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
   // tracks to follow in the next iteration (Kernel.cl:344-355)
   const bool push = action == kPushTrack || action == kNewTrack || action == kPushSkip;
   const uint32_t slot = warp_reserve(&s.ring_lo[nb], push);
-  if (push && slot < ev.ring_cap) ring_buf(ev, nb)[slot] = push_value;
+  if (push && slot < ev.ring_cap)   // a skip keeps the hits; a new hit shifts them
+    ring_buf(ev, nb)[slot] = action == kPushSkip ? make_uint4(push_value, en.y, en.z, en.w)
+                                                 : make_uint4(push_value, 0u, en.w, best_h2);
   // three-hit tracklets that ran out of skips (Kernel.cl:359-363)
   const uint32_t wi = warp_reserve(&s.nweak, action == kWeak);
   if (action == kWeak && wi < ev.cap) ev.weak[wi] = trackno;
@@ -567,7 +562,7 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
       const uint32_t tp = atomicAdd(&s.ntracklets, 1u);
       if (tp < ev.cap) {
         ev.tracklets[tp] = make_uint4((uint32_t)h0, h1, h2, 0u);
-        push_back(s, ev, nb, kTrackletFlag | tp);
+        push_back(s, ev, nb, make_uint4(kTrackletFlag | tp, (uint32_t)h0, h1, h2));
       }
     }
   }
@@ -621,7 +616,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   ev.narrow = p.narrow != 0;
   const int S = ev.S, H = ev.H;
   ev.cap = H > 0 ? (uint32_t)H : 1u;
-  ev.ring_cap = (uint32_t)H + 1u;
+  ev.ring_cap = ev.cap;
   const int32_t* gZ = hdr + 2;
   const int32_t* gstart = gZ + S;
   const int32_t* gnum = gstart + S;
@@ -636,9 +631,9 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   ev.z = reinterpret_cast<float*>(arena + L.z);
   ev.win = reinterpret_cast<uint2*>(arena + L.win);
   ev.used = arena + L.used;
-  ev.ring0 = reinterpret_cast<uint32_t*>(arena + L.ring0);
-  ev.ring1 = reinterpret_cast<uint32_t*>(arena + L.ring1);
   const uint64_t hb = p.hit_base[e];
+  ev.ring0 = reinterpret_cast<uint4*>(p.rings + 8 * hb);
+  ev.ring1 = ev.ring0 + ev.cap;
   ev.tracklets = reinterpret_cast<uint4*>(p.tracklets + 4 * hb);
   ev.weak = p.weak + hb;
   ev.tracks = p.tracks + hb;
@@ -781,7 +776,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       const uint32_t lo_n = min(s.ring_lo[b], ev.ring_cap);
       const uint32_t ncur = min(lo_n + s.ring_hi[b], ev.ring_cap);
       for (uint32_t i = tid; i < ncur; i += nt) {
-        const uint32_t v = ring_entry(ev, b, lo_n, i);
+        const uint32_t v = ring_entry(ev, b, lo_n, i).x;
         if (v & kTrackletFlag) {
           const uint32_t wi = atomicAdd(&s.nweak, 1u);
           if (wi < ev.cap) ev.weak[wi] = v & kEntryNumber;

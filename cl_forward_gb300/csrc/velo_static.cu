@@ -13,7 +13,7 @@
 //   n_events                      <= VELO_STATIC_MAX_EVENTS
 //   total_hits + n_events         <= VELO_STATIC_MAX_HIT_ROWS
 //   max_event_hits                small enough for the event to be staged in
-//                                 shared memory (7,731 hits)
+//                                 shared memory (10,676 hits)
 // and on the device (events that break them get VELO_EVENT_INVALID and no
 // tracks; nothing is written out of bounds): each event's header and module
 // table are checked as the host path checks them, and its hit count must not
@@ -35,7 +35,7 @@
 namespace velo {
 namespace {
 
-constexpr uint64_t kRowBytes = 16u + 4u + sizeof(velo_track);   // tracklet + weak + track per hit row
+constexpr uint64_t kRowBytes = 16u + 32u + 4u + sizeof(velo_track);   // tracklet + rings + weak + track per hit row
 constexpr uint64_t kEventBytes = 4u + 4u + 4u + 8u + 8u;         // hits, maxmod, valid, hit_base, arena_off
 constexpr uint64_t kCounterBytes = 256;
 constexpr uint64_t kOffEvents = kCounterBytes;
@@ -53,6 +53,7 @@ struct StaticView {
   uint64_t* hit_base;
   uint64_t* arena_off;
   uint32_t* tracklets;          // 4 words per row
+  uint32_t* rings;              // 8 words per row
   uint32_t* weak;               // 1 per row
   velo_track* tracks;           // 1 per row
 };
@@ -71,6 +72,7 @@ __host__ __device__ StaticView view_of(uint8_t* base) {
   v.tracks = reinterpret_cast<velo_track*>(rows);
   v.tracklets = reinterpret_cast<uint32_t*>(rows + sizeof(velo_track) * VELO_STATIC_MAX_HIT_ROWS);
   v.weak = reinterpret_cast<uint32_t*>(rows + (sizeof(velo_track) + 16u) * VELO_STATIC_MAX_HIT_ROWS);
+  v.rings = reinterpret_cast<uint32_t*>(rows + (sizeof(velo_track) + 20u) * VELO_STATIC_MAX_HIT_ROWS);
   return v;
 }
 
@@ -204,6 +206,7 @@ extern "C" velo_status velo_search_device_static(const uint8_t* d_input, const u
   p.smem_arena_bytes = smem;
   p.global_arena = nullptr;
   p.tracklets = v.tracklets;
+  p.rings = v.rings;
   p.weak = v.weak;
   p.tracks = v.tracks;
   p.out_tracks = d_tracks_out;

@@ -265,13 +265,13 @@ int32_t velo_device_sm_count(const velo_ctx* ctx);
  * NULL = the legacy default stream) and the results are valid once it is
  * synchronised.  Y-lanes as in velo_options; narrowing is on.
  *
- * All other memory is one file-scope device array of about 16 MB per GPU,
+ * All other memory is one file-scope device array of about 20 MB per GPU,
  * held from library load to process exit.  Limits per call, rejected with
  * VELO_ERR_CAPACITY: n_events <= VELO_STATIC_MAX_EVENTS;
  * total_hits + n_events <= VELO_STATIC_MAX_HIT_ROWS (total_hits = the sum of
  * the events' hit counts); track_capacity >= total_hits + n_events;
  * max_event_hits (an upper bound on any event's hit count) small enough to
- * stage the event in shared memory: 7,731 hits.  Events that break
+ * stage the event in shared memory: 10,676 hits.  Events that break
  * their declared bounds get VELO_EVENT_INVALID and no tracks.
  *
  * The first call on a device takes the array's device address (with that

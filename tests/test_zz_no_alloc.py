@@ -74,7 +74,7 @@ def test_static_matches_allocating_entry_point_on_consecutive_calls(lib_and_ctx)
     from cl_forward_gb300 import fuzz, generator, native
     lib, ctx = lib_and_ctx
     batch_a = [native.sort_by_x(b) for b in generator.generate(range(30))[0]]
-    # denser events, within the entry point's per-event limit (7,731 hits)
+    # denser events, within the entry point's per-event limit (10,676 hits)
     dense = generator.generate(range(50, 90), generator.CONFIG_BATCHED)[0]
     batch_b = [native.sort_by_x(b) for b in dense if _hits(b) <= 3200]
     assert len(batch_b) >= 5
