@@ -156,19 +156,42 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
       const float D = fmul(kMaxXSlopeCandidates, fmaxf(da, db));   // >= every hit's dxmax
       narrow_range(x2, 0, n2, x0, x0, D, &lo, &hi);
     }
-    bool found = false;
-    for (int e = lo; e < hi; ++e) {
-      const float h_dist = fabsf(fsub(z2[e], z0));
-      const float dxmax = fmul(kMaxXSlopeCandidates, h_dist);
-      const bool tol = fabsf(fsub(x2[e], x0)) < dxmax;
-      if (!found) {
-        if (tol) { found = true; r1f = (uint32_t)e; }
-      } else if (!tol) {
-        r1l = (uint32_t)e;
-        break;
+    if (sorted && n2 > 0 && s.zmin[s2] == s.zmax[s2]) {
+      // one z on the module: dxmax is the same for every hit, and
+      // d = fl(x2 - x0) is non-decreasing in x2, so the hits passing
+      // |d| < dxmax are exactly [A, B): A = first with d > -dxmax, B = first
+      // with d >= dxmax -- the scan's first pass and first later failure
+      const float dxmax = fmul(kMaxXSlopeCandidates, fabsf(fsub(z2[0], z0)));
+      int a = lo, b = hi;
+      while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (fsub(x2[mid], x0) > -dxmax) b = mid; else a = mid + 1;
       }
+      const int A = a;
+      b = hi;
+      while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (!(fsub(x2[mid], x0) < dxmax)) b = mid; else a = mid + 1;
+      }
+      if (A < a) {
+        r1f = (uint32_t)A;
+        r1l = (uint32_t)a;   // a == hi: hit `hi` provably fails, or hi is the end
+      }
+    } else {
+      bool found = false;
+      for (int e = lo; e < hi; ++e) {
+        const float h_dist = fabsf(fsub(z2[e], z0));
+        const float dxmax = fmul(kMaxXSlopeCandidates, h_dist);
+        const bool tol = fabsf(fsub(x2[e], x0)) < dxmax;
+        if (!found) {
+          if (tol) { found = true; r1f = (uint32_t)e; }
+        } else if (!tol) {
+          r1l = (uint32_t)e;
+          break;
+        }
+      }
+      if (found && r1l == kNone16) r1l = (uint32_t)hi;   // hit `hi` provably fails, or hi is the end
     }
-    if (found && r1l == kNone16) r1l = (uint32_t)hi;   // hit `hi` provably fails, or hi is the end
   }
 
   // h2 window for h taken as the h1 of a seed on f+2 (Kernel.cl:85-102,137-150).
