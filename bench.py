@@ -66,7 +66,8 @@ def parse_args():
     ap.add_argument("--threads", type=int, default=256)
     ap.add_argument("--smem-hits", type=int, default=0)
     ap.add_argument("--no-narrow", action="store_true")
-    ap.add_argument("--register-ctas", type=int, default=5, choices=[4, 5])
+    ap.add_argument("--register-ctas", type=int, default=0, choices=[0, 4, 5, 18],
+                    help="register build (0: automatic for the thread count)")
     ap.add_argument("--graph", action="store_true", help="replay launches from a CUDA graph")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the library's default launch configuration instead of the autotuned one")

@@ -20,7 +20,7 @@ CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "auto
 FIELDS = ("threads_per_event", "launch_mode", "smem_hits", "narrow_windows", "register_ctas")
 
 
-SPACE = 5   # bumped when velo_autotune's candidate set changes: older entries are ignored
+SPACE = 6   # bumped when velo_autotune's candidate set changes: older entries are ignored
 
 
 def shape_key(sm_count: int, n_events: int, mean_hits: float, y_lanes: int) -> str:

@@ -60,13 +60,10 @@ int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
   std::vector<uint32_t> counts(eventsToProcess), status(eventsToProcess);
   std::vector<uint64_t> first(eventsToProcess);
   velo_options opts;
-  velo_default_options(&opts);   // Y = 4: the reference's output configuration
-  // persistent CTAs of 128 threads pulling events largest-first, and copies
-  // overlapped with the search in parts of 2,500 events: the fastest
-  // configuration measured for batches of thousands of events
-  opts.launch_mode = VELO_LAUNCH_PERSISTENT;
-  opts.threads_per_event = 128;
-  opts.register_ctas = 4;
+  // Y = 4 (the reference's output configuration), persistent 64-thread CTAs;
+  // the caller's vectors are pageable, so copies overlap the search in parts
+  // of 2,500 events
+  velo_default_options(&opts);
   opts.pipeline_events = 2500;
   velo_status st = velo_search(c, ptrs.data(), sizes.data(), eventsToProcess, &opts, tracks.data(), cap,
                                counts.data(), first.data(), status.data());

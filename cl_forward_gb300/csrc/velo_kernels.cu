@@ -856,9 +856,10 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   VELO_PHASE_END();
 }
 
-// Three instantiations: up to 256 threads per CTA with registers budgeted
-// for 4 or for 5 resident CTAs per SM (velo_options.register_ctas), and
-// 512-thread CTAs.
+// Instantiations: up to 256 threads per CTA with registers budgeted for 4 or
+// for 5 resident 256-thread CTAs per SM (velo_options.register_ctas 4 / 5:
+// 64 / 48 registers), 64-thread CTAs with 56 registers (18 CTAs per SM,
+// register_ctas 18), and 512-thread CTAs.
 template <int kMaxThreads, int kMinCtas, int kMode, int kMods>
 __global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const SearchParams p) {
   extern __shared__ __align__(16) uint8_t dyn_smem_raw[];
@@ -892,6 +893,8 @@ constexpr int kFullModules = kMaxModules + 1;
 #define VELO_KERNEL_R5 search_kernel<256, 5, kPlain, kFullModules>
 #define VELO_KERNEL_R4C search_kernel<256, 4, kPlain, kCompactModules>
 #define VELO_KERNEL_R5C search_kernel<256, 5, kPlain, kCompactModules>
+#define VELO_KERNEL_R18 search_kernel<64, 18, kPlain, kFullModules>
+#define VELO_KERNEL_R18C search_kernel<64, 18, kPlain, kCompactModules>
 #define VELO_KERNEL_LARGE search_kernel<512, 1, kPlain, kFullModules>
 #define VELO_KERNEL_DUMP search_kernel<256, 4, kDump, kFullModules>
 #define VELO_KERNEL_LEARNED search_kernel<256, 4, kLearned, kFullModules>
@@ -908,6 +911,10 @@ int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_byte
     VELO_KERNEL_DUMP<<<grid, min(block, 256), smem_bytes, st>>>(p);
   else if (block > 256)
     VELO_KERNEL_LARGE<<<grid, block, smem_bytes, st>>>(p);
+  else if (reg_ctas == 18 && compact)
+    VELO_KERNEL_R18C<<<grid, block, smem_bytes, st>>>(p);
+  else if (reg_ctas == 18)
+    VELO_KERNEL_R18<<<grid, block, smem_bytes, st>>>(p);
   else if (reg_ctas == 4 && compact)
     VELO_KERNEL_R4C<<<grid, block, smem_bytes, st>>>(p);
   else if (reg_ctas == 4)
@@ -933,6 +940,10 @@ int configure_search_kernel(uint32_t smem_bytes) {
     e = cudaFuncSetAttribute(VELO_KERNEL_R5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(VELO_KERNEL_R4C, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_R18, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(VELO_KERNEL_R18C, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(VELO_KERNEL_R5C, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e == cudaSuccess)
@@ -966,6 +977,9 @@ int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, boo
                                                               smem_bytes);
   if (block > 256)
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, VELO_KERNEL_LARGE, block, smem_bytes);
+  if (reg_ctas == 18)
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        ctas_per_sm, compact ? VELO_KERNEL_R18C : VELO_KERNEL_R18, block, smem_bytes);
   if (reg_ctas == 4)
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, compact ? VELO_KERNEL_R4C : VELO_KERNEL_R4,
                                                               block, smem_bytes);

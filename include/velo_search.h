@@ -88,7 +88,9 @@ typedef struct velo_options {
   int32_t ctas_per_sm;        /* persistent mode: resident CTAs per SM; 0 = auto */
   int32_t use_graph;          /* 1: capture the launch sequence in a CUDA graph and replay it */
   int32_t register_ctas;      /* 4 or 5: kernel build whose registers fit that many 256-thread
-                                 CTAs per SM (fewer registers, more CTAs); 0 = 5 */
+                                 CTAs per SM (64 or 48 registers); 18: the 64-thread build with
+                                 56 registers (18 CTAs per SM; threads_per_event <= 64 only);
+                                 0 = 18 for <= 64 threads, else 5 */
   int32_t learned;            /* 1: seeding prunes doublets with the MLP set by velo_set_mlp
                                  (approximate; no counterpart in the reference) */
   int32_t pipeline_events;    /* velo_search / velo_search_packed: > 0 cuts a batch of more than
@@ -123,6 +125,9 @@ typedef struct velo_stats {
 
 typedef struct velo_ctx velo_ctx;
 
+/* Defaults: Y = 4, persistent CTAs of 64 threads, 50-hit shared-memory
+ * tile, narrowing on, automatic register build, no graph, no pipelining, no
+ * in-place host I/O, plain (not learned) seeding. */
 void velo_default_options(velo_options* opts);
 const char* velo_status_string(velo_status s);
 

@@ -93,6 +93,14 @@ def test_register_builds_and_graph_replay(gpu_ctx, oracle_lib):
     for regs in (4, 5):
         _assert_same(gpu_ctx, oracle_lib, blobs, register_ctas=regs)
         _assert_same(gpu_ctx, oracle_lib, blobs, register_ctas=regs, use_graph=1, launch_mode=1)
+    # the 56-register 64-thread build, one CTA per event and persistent, with and without a tile
+    for mode in (0, 1):
+        for hits in (0, 50):
+            _assert_same(gpu_ctx, oracle_lib, blobs, register_ctas=18, threads_per_event=64, launch_mode=mode,
+                         smem_hits=hits)
+    from cl_forward_gb300 import native
+    with pytest.raises(native.VeloError):                   # the 64-thread build takes 64 threads only
+        gpu_ctx.search(blobs, native.default_options(register_ctas=18, threads_per_event=128))
 
 
 def test_graph_replays_on_staged_events(gpu_ctx, oracle_lib):

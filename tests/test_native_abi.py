@@ -117,6 +117,8 @@ def test_context_without_gpu_fails_loudly(native_lib):
 def test_default_options(native_lib):
     from cl_forward_gb300 import native
     o = native.default_options()
-    assert o.y_lanes == 4 and o.threads_per_event == 256 and o.narrow_windows == 1
-    o = native.default_options(y_lanes=2, launch_mode=native.LAUNCH_PERSISTENT)
-    assert o.y_lanes == 2 and o.launch_mode == 1
+    assert o.y_lanes == 4 and o.threads_per_event == 64 and o.narrow_windows == 1
+    assert o.launch_mode == native.LAUNCH_PERSISTENT and o.smem_hits == 50 and o.register_ctas == 0
+    assert o.learned == 0 and o.pipeline_events == 0 and o.host_direct == 0 and o.use_graph == 0
+    o = native.default_options(y_lanes=2, launch_mode=native.LAUNCH_PER_EVENT)
+    assert o.y_lanes == 2 and o.launch_mode == 0
