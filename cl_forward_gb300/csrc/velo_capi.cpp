@@ -988,11 +988,57 @@ velo_status search_pipelined(velo_ctx* c, const uint8_t* buf, const uint64_t* of
 
 }  // namespace
 
+namespace {
+
+// Upper bound of the device bytes one event takes in a staged batch, from its
+// blob size alone (H <= (size - 8) / 16): per hit row 152 B of scratch
+// (tracklet, rings, weak, working track), 100 B of output and 21 B of arena,
+// plus the blob itself and its metadata.
+uint64_t event_device_bytes(uint64_t size) {
+  const uint64_t rows = std::max<uint64_t>(size >= 8 ? (size - 8) / 16 : 0, 1);
+  return rows * (152 + 100 + 21) + size + 64;
+}
+
+// Events per part when the batch would not fit the device budget, else 0.
+int32_t budget_part(velo_ctx* c, const uint64_t* sizes, int32_t n, int32_t budget_mb) {
+  if (n < 2) return 0;
+  uint64_t need = 0;
+  for (int32_t e = 0; e < n; ++e) need += event_device_bytes(sizes[e]);
+  uint64_t budget = (uint64_t)budget_mb << 20;
+  if (budget_mb <= 0) {
+    if (need < (256ull << 20)) return 0;   // small batches never ask the driver
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    budget = free_b / 2;
+  }
+  if (need <= budget) return 0;
+  // two parts are in flight at a time, each in its own child context
+  const uint64_t part = (uint64_t)n * (budget / 2) / need;
+  return (int32_t)std::max<uint64_t>(part, 1);
+}
+
+}  // namespace
+
 velo_status velo_search_packed(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
                                const uint64_t* sizes, int32_t n, const velo_options* opts,
                                velo_track* tracks_out, uint64_t capacity, uint32_t* counts,
                                uint64_t* first, uint32_t* status) {
   if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  if (!opts || opts->pipeline_events <= 0) {
+    const int32_t part = budget_part(c, sizes, n, opts ? opts->device_budget_mb : 0);
+    if (part > 0) {   // too large for one staging: pipelined parts that fit
+      velo_options o;
+      velo_status st = check_options(c, opts, &o);
+      if (st != VELO_OK) return st;
+      VELO_CUDA(c, cudaSetDevice(c->device));
+      o.pipeline_events = part;
+      if (n <= 2 * part) o.pipeline_events = (n + 2) / 3;   // at least three parts
+      return search_pipelined(c, buf, offsets, sizes, n, o, tracks_out, capacity, counts, first, status);
+    }
+  }
   if (opts && opts->pipeline_events > 0 && n > 2 * opts->pipeline_events) {
     velo_options o;
     velo_status st = check_options(c, opts, &o);

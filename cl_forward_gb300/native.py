@@ -67,7 +67,8 @@ class Options(ctypes.Structure):
                 ("narrow_windows", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("register_ctas", ctypes.c_int32),
                 ("learned", ctypes.c_int32), ("pipeline_events", ctypes.c_int32),
-                ("host_direct", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("host_direct", ctypes.c_int32), ("device_budget_mb", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 class Stats(ctypes.Structure):

@@ -103,7 +103,10 @@ typedef struct velo_options {
                                  place over the host link instead of staging copies; other
                                  buffers are copied as usual.  Results are identical; the
                                  context holds no staged batch afterwards.  0 = off */
-  int32_t reserved[5];
+  int32_t device_budget_mb;   /* velo_search / velo_search_packed: device memory one call may
+                                 use; a batch that needs more (about 275 B per hit) is cut into
+                                 pipelined parts that fit.  0 = half the free device memory */
+  int32_t reserved[4];
 } velo_options;
 
 typedef struct velo_stats {

@@ -330,3 +330,17 @@ def test_host_direct_io_matches_copies(gpu_ctx, oracle_lib, part):
                                    np.zeros(n, np.uint64), np.zeros(n, np.uint32))
     gpu_ctx.host_free(pinned)
     gpu_ctx.host_free(ptracks.view(np.uint8))
+
+
+def test_device_budget_splits_large_batches(gpu_ctx, oracle_lib):
+    """A batch needing more device memory than the call's budget is cut into
+    pipelined parts: same tracks and statuses, one contiguous output."""
+    from cl_forward_gb300 import generator, native
+    blobs = _sorted(oracle_lib, generator.generate(range(7000, 7300))[0])
+    whole, st1 = gpu_ctx.search(blobs, native.default_options())
+    for direct in (0, 1):
+        parts, st2 = gpu_ctx.search(blobs, native.default_options(device_budget_mb=8, host_direct=direct))
+        assert np.array_equal(st1, st2)
+        assert gpu_ctx.stats().launches > 2                  # it was split
+        for e in range(len(blobs)):
+            assert index_lists(parts[e]) == index_lists(whole[e])
