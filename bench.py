@@ -2,8 +2,8 @@
 """Throughput of the GB300 search-by-triplet (events/s) on seeded synthetic VELO events.
 
 Default workload: 10,000 events from seeds 1000..10999 of the synthetic VELO
-generator (the plain path at scale: one CTA per event, Y = 4, no FMA
-contraction), x-sorted by the reference sort before timing.
+generator (the plain path at scale, Y = 4, no FMA contraction), x-sorted by
+the reference sort before timing.
 
 The launch configuration is the autotuner's (velo_autotune: threads per
 event, shared-memory tile, register build, launch style; cached per workload
@@ -13,14 +13,18 @@ Per step the GPU arm searches the whole batch once:
   value  device-resident: one kernel launch over events already in HBM, timed
          with CUDA events on the library's stream; L2 is flushed between steps
          (a 2 x L2 memset) and the input is also larger than L2.
-  e2e    the public C ABI (velo_search_packed) from pinned host memory:
-         H2D of the events, the kernel, D2H of counts / offsets / status /
-         tracks, all inside the timed region (host wall clock).
+  e2e    the public C ABI (velo_search_packed) from pinned host buffers: the
+         kernel reads the events and writes the tracks in place over the host
+         link (host_direct; --e2e-copies for H2D / D2H copies instead), plus
+         the D2H of counts / offsets / status, all inside the timed region
+         (host wall clock).
   cpu_baseline  the oracle restatement of the reference algorithm on all host
          cores over a bounded sample (rank 0 only).
+  learned  the learned-pruned search of the same events (committed weights).
 `--impl reference` times the reference's algorithm on the host CPU instead:
-the reference kernel under the work-group emulator where it was built
-(oracle/_ref), else the oracle restatement.
+the oracle restatement on all host cores, or with --ref-emulator the
+reference kernel itself under the work-group emulator (only where it was
+built from the reference sources).
 
 Multi-GPU (torchrun): weak scaling, every rank searches its own 10,000-event
 block (seeds offset by rank); no collective touches the data path, only a
@@ -44,9 +48,8 @@ METRIC = "events/s on 1 GB300: plain vs learned-pruned at <=0.5% eff loss; vs re
 
 CONFIGS = {
     # name: (first seed, events, generator params attr, launch mode, description)
-    "scale": (1000, 10000, "CONFIG_SCALE", 0,
-              "10,000 synthetic VELO events (seeds 1000-10999), plain path, one CTA per event"),
-    "small": (0, 100, "CONFIG_SMALL", 0, "100 synthetic VELO events (seeds 0-99), one CTA per event"),
+    "scale": (1000, 10000, "CONFIG_SCALE", 1, "10,000 synthetic VELO events (seeds 1000-10999), plain path"),
+    "small": (0, 100, "CONFIG_SMALL", 1, "100 synthetic VELO events (seeds 0-99), plain path"),
     "batched": (2000000, 100000, "CONFIG_BATCHED", 1,
                 "100,000 uneven events, PVs ~ Poisson(U(2,30)), persistent CTAs"),
     "stress": (3000000, 100000, "CONFIG_STRESS", 1,
@@ -63,8 +66,8 @@ def parse_args():
     ap.add_argument("--config", choices=sorted(CONFIGS), default="scale")
     ap.add_argument("--events", type=int, default=0, help="override the number of events")
     ap.add_argument("--launch", choices=["per-event", "persistent"], default=None)
-    ap.add_argument("--threads", type=int, default=256)
-    ap.add_argument("--smem-hits", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=64)
+    ap.add_argument("--smem-hits", type=int, default=50)
     ap.add_argument("--no-narrow", action="store_true")
     ap.add_argument("--register-ctas", type=int, default=0, choices=[0, 4, 5, 18],
                     help="register build (0: automatic for the thread count)")
