@@ -82,6 +82,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-pruning leg")
+    ap.add_argument("--no-stages", action="store_true", help="skip the device sort / fit leg")
     ap.add_argument("--ref-emulator", action="store_true",
                     help="reference arm: time the reference kernel under the work-group emulator "
                          "(oracle/_ref, only where it was built) instead of the oracle restatement")
@@ -314,6 +315,51 @@ def profiled_traffic(config: str, n_events: int):
     return None, None
 
 
+def stages_leg(ctx, raw, opts, n_tracks_expected):
+    """The stages either side of the search, on the GPU: the device x-sort of
+    the unsorted events (the reference sorts on the host before every launch),
+    then the search of the device-sorted events and the straight-line fit of
+    every output track.  Host wall clock with a synchronize on both sides."""
+    import numpy as np
+    n = len(raw)
+    offs = np.zeros(n, np.uint64)
+    sizes = np.array([len(b) for b in raw], np.uint64)
+    total = 0
+    for i, b in enumerate(raw):
+        offs[i] = total
+        total += (len(b) + 15) // 16 * 16
+    hbuf = ctx.host_alloc(max(total, 16))
+    for i, b in enumerate(raw):
+        hbuf[int(offs[i]):int(offs[i]) + len(b)] = np.frombuffer(b, np.uint8)
+    sort_s = []
+    for _ in range(3):   # the sort works in place: staged afresh each time
+        ctx.stage(hbuf, offs, sizes)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.sort_staged()
+        ctx.synchronize()
+        sort_s.append(time.perf_counter() - t0)
+    o = type(opts).from_buffer_copy(opts)
+    o.use_graph = 0
+    ctx.run(o)
+    rows = int(sum(max(int(np.frombuffer(b[4:8], "<i4")[0]), 1) for b in raw))
+    _, counts, _, _ = ctx.fetch(n, rows)
+    total_tracks = int(counts.sum())
+    fit_s = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        fits = ctx.fit_tracks(total_tracks)
+        fit_s.append(time.perf_counter() - t0)
+    ctx.host_free(hbuf)
+    sort_ms, fit_ms = 1e3 * statistics.median(sort_s), 1e3 * statistics.median(fit_s)
+    return {"device_sort": {"ms": sort_ms, "events_per_s": n / (sort_ms / 1e3)},
+            "fit": {"ms": fit_ms, "tracks_per_s": total_tracks / (fit_ms / 1e3),
+                    "note": "includes the device-to-host copy of the fits (20 B per track)"},
+            "tracks_after_device_sort": total_tracks,
+            "same_track_count_as_host_sort": total_tracks == n_tracks_expected,
+            "fits_finite": bool(np.isfinite(fits["x0"][:total_tracks]).all())}
+
+
 LEARNED_WEIGHTS = os.path.join(ROOT, "cl_forward_gb300", "weights", "doublet_mlp.npz")
 
 
@@ -488,6 +534,8 @@ def gpu_arm(args, ranks: Ranks):
         "status_flags": {"ring_overflow": int(np.sum(status & 1 != 0)),
                          "track_overflow": int(np.sum(status & 2 != 0))},
     }
+    if not args.no_stages:
+        line["pipeline_stages"] = stages_leg(ctx, raw, opts, int(T.sum()))
     if not args.no_learned and os.path.exists(LEARNED_WEIGHTS):
         line["learned"] = learned_leg(ctx, hbuf, offs, sizes, blobs, truths, opts, tracks, counts, first, ms,
                                       args)

@@ -11,7 +11,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <algorithm>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/GpuPixelSearchByTriplet.h"
@@ -97,14 +100,32 @@ int gpuPixelSearchByTripletInvocation(const std::vector<const std::vector<uint8_
 }
 
 void preorder_by_x(std::vector<const std::vector<uint8_t>*>& input) {
-  for (const std::vector<uint8_t>* ev : input) {
-    if (!ev || ev->empty()) continue;
-    // The reference sorts the caller's buffers in place through const
-    // pointers (Tools.cpp:51-63); so does this.
-    uint8_t* blob = const_cast<uint8_t*>(ev->data());
-    velo_status st = velo_sort_by_x(blob, ev->size());
-    if (st != VELO_OK) fail("preorder_by_x", st, nullptr);
+  // The reference sorts the caller's buffers in place through const
+  // pointers (Tools.cpp:51-63), one event after another; so does this, with
+  // the events spread over the host's cores (each event is independent, and
+  // each event's permutation is the reference's).
+  const size_t n = input.size();
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t workers = std::min<size_t>(hw, (n + 63) / 64);
+  std::atomic<size_t> next{0};
+  std::atomic<int> bad{0};
+  auto work = [&]() {
+    for (size_t i; (i = next.fetch_add(1)) < n;) {
+      const std::vector<uint8_t>* ev = input[i];
+      if (!ev || ev->empty()) continue;
+      uint8_t* blob = const_cast<uint8_t*>(ev->data());
+      const velo_status st = velo_sort_by_x(blob, ev->size());
+      if (st != VELO_OK) bad.store((int)st);
+    }
+  };
+  if (workers <= 1) {
+    work();
+  } else {
+    std::vector<std::thread> pool;
+    for (size_t t = 0; t < workers; ++t) pool.emplace_back(work);
+    for (std::thread& t : pool) t.join();
   }
+  if (bad.load() != 0) fail("preorder_by_x", (velo_status)bad.load(), nullptr);
 }
 
 int independent_execute(const std::vector<std::vector<uint8_t> >& input,

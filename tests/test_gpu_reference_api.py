@@ -64,3 +64,30 @@ def test_cpp_driver_dump(native_lib, oracle_lib, tmp_path):
         ev = events.unpack_event(oracle_lib.sort_by_x(raw[i]))
         ref_ids = sorted(tuple(sorted(int(ev.hit_id[h]) for h in t)) for t in index_lists(want[i]))
         assert ids == ref_ids
+
+
+def test_cpp_driver_sorts_many_events_in_parallel(native_lib, oracle_lib, tmp_path):
+    """independent_execute through the C++ driver on 150 events: the host
+    sort then runs on several threads; every event keeps the reference's
+    permutation, so the dumped tracks match the oracle's on the sorted events."""
+    from cl_forward_gb300 import build, events, generator
+    raw = generator.generate(range(300, 450))[0]
+    data = tmp_path / "data"
+    dump = tmp_path / "dump"
+    data.mkdir()
+    dump.mkdir()
+    for i, b in enumerate(raw):
+        events.write_dat(str(data / f"{i:03d}.dat"), b)
+    r = subprocess.run([build.DRIVER, str(data), str(len(raw)), "--dump", str(dump)], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    want, _ = oracle_lib.search([oracle_lib.sort_by_x(b) for b in raw], 4)
+    names = sorted(os.listdir(str(data)))
+    for i, name in enumerate(names):
+        e = int(name.split(".")[0])
+        text = (dump / f"{i}.out").read_text()
+        tracks = re.findall(r"Track #(\d+), length (\d+)\n(.*?)\n\n", text, re.S)
+        ids = sorted(tuple(sorted(int(m) for m in re.findall(r"^\s+(\d+) \(", body, re.M)))
+                     for _, _, body in tracks)
+        ev = events.unpack_event(oracle_lib.sort_by_x(raw[e]))
+        assert ids == sorted(tuple(sorted(int(ev.hit_id[h]) for h in t)) for t in index_lists(want[e]))
