@@ -84,14 +84,16 @@ void dump_event(const std::string& path, const std::vector<uint8_t>& ev, const s
 int main(int argc, char* argv[]) {
   std::string folder, dump_dir;
   size_t n_files = 50;   // IndependentEntrypoint.cpp:142
+  int repeat = 1;        // > 1: run the batch again (steady state: context and buffers reused)
   std::vector<std::string> pos;
   for (int i = 1; i < argc; ++i) {
     if (std::strcmp(argv[i], "--dump") == 0 && i + 1 < argc) dump_dir = argv[++i];
+    else if (std::strcmp(argv[i], "--repeat") == 0 && i + 1 < argc) repeat = std::max(1, std::atoi(argv[++i]));
     else pos.emplace_back(argv[i]);
   }
   if (pos.empty()) {
     std::cerr << "Usage: " << argv[0] << " <folder including .dat files> [number of files to process=50]"
-              << " [--dump DIR]" << std::endl;
+              << " [--dump DIR] [--repeat K]" << std::endl;
     return -1;
   }
   folder = pos[0];
@@ -124,7 +126,10 @@ int main(int argc, char* argv[]) {
   }
   std::cout << input.size() << " files read" << std::endl;
   std::vector<std::vector<uint8_t>> output;
-  independent_execute(input, output);
+  for (int r = 0; r < repeat; ++r) {
+    output.clear();
+    independent_execute(input, output);
+  }
   if (!dump_dir.empty())
     for (size_t i = 0; i < output.size(); ++i)
       dump_event(dump_dir + "/" + std::to_string(i) + ".out", input[i], output[i]);

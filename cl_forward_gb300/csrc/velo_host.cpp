@@ -13,6 +13,7 @@
 #include <iostream>
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -25,6 +26,27 @@ namespace {
 int g_verbosity = 0;   // 3 in standalone mode, 0 in framework mode (GpuPixelSearchByTriplet.cpp:16,35)
 velo_ctx* g_ctx = nullptr;
 std::mutex g_mutex;
+// pinned track buffer the kernel writes in place, kept between calls
+velo_track* g_tracks = nullptr;
+uint64_t g_tracks_cap = 0;
+
+// Runs f(a, b) over [0, n) on the host's cores when n is large.
+template <class F>
+void parallel_for(size_t n, size_t grain, F f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t workers = std::min<size_t>(hw, (n + grain - 1) / grain);
+  if (workers <= 1) {
+    f((size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const size_t chunk = (n + workers - 1) / workers;
+  for (size_t t = 0; t < workers; ++t) {
+    const size_t a = t * chunk, b = std::min(n, a + chunk);
+    if (a < b) pool.emplace_back(f, a, b);
+  }
+  for (std::thread& t : pool) t.join();
+}
 
 [[noreturn]] void fail(const char* where, velo_status st, const char* detail) {
   std::cerr << "Error in function " << where << std::endl
@@ -59,23 +81,36 @@ int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
     sizes[i] = v->size();
   }
   const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), eventsToProcess);
-  std::vector<velo_track> tracks(cap);
+  if (cap > g_tracks_cap) {   // grow-only, not zero-filled: only [first, first + count) is read
+    if (g_tracks) velo_host_free(c, g_tracks);
+    g_tracks = nullptr;
+    g_tracks_cap = 0;
+    void* p = nullptr;
+    const uint64_t want = cap + cap / 4;
+    velo_status st = velo_host_alloc(c, want * sizeof(velo_track), &p);
+    if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
+    g_tracks = static_cast<velo_track*>(p);
+    g_tracks_cap = want;
+  }
+  velo_track* tracks = g_tracks;
   std::vector<uint32_t> counts(eventsToProcess), status(eventsToProcess);
   std::vector<uint64_t> first(eventsToProcess);
   velo_options opts;
   // Y = 4 (the reference's output configuration), persistent 64-thread CTAs;
-  // the caller's vectors are pageable, so copies overlap the search in parts
-  // of 2,500 events
+  // the events are gathered into the context's pinned buffer and the tracks
+  // land in the pinned track buffer, both accessed by the kernel in place
   velo_default_options(&opts);
-  opts.pipeline_events = 2500;
-  velo_status st = velo_search(c, ptrs.data(), sizes.data(), eventsToProcess, &opts, tracks.data(), cap,
+  opts.host_direct = 1;
+  velo_status st = velo_search(c, ptrs.data(), sizes.data(), eventsToProcess, &opts, tracks, g_tracks_cap,
                                counts.data(), first.data(), status.data());
   if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
-  for (int i = 0; i < eventsToProcess; ++i) {
-    std::vector<uint8_t>& out = output[startingEvent + i];
-    out.resize((size_t)counts[i] * sizeof(velo_track));
-    if (counts[i]) std::memcpy(out.data(), &tracks[first[i]], out.size());
-  }
+  parallel_for((size_t)eventsToProcess, 512, [&](size_t a, size_t b) {
+    for (size_t i = a; i < b; ++i) {
+      std::vector<uint8_t>& out = output[startingEvent + i];
+      out.resize((size_t)counts[i] * sizeof(velo_track));
+      if (counts[i]) std::memcpy(out.data(), &tracks[first[i]], out.size());
+    }
+  });
   if (g_verbosity >= 3) {
     velo_stats s;
     velo_get_stats(c, &s);
@@ -133,8 +168,17 @@ int independent_execute(const std::vector<std::vector<uint8_t> >& input,
   std::vector<const std::vector<uint8_t>*> converted(input.size());
   for (size_t i = 0; i < input.size(); ++i) converted[i] = &input[i];
   g_verbosity = 3;
+  const auto t0 = std::chrono::steady_clock::now();
   preorder_by_x(converted);
-  return gpuPixelSearchByTripletInvocation(converted, output);
+  const auto t1 = std::chrono::steady_clock::now();
+  const int r = gpuPixelSearchByTripletInvocation(converted, output);
+  const auto t2 = std::chrono::steady_clock::now();
+  const double sort_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  const double search_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+  std::cout << "Sorted " << input.size() << " events on the host in " << sort_ms << " ms; searched them in "
+            << search_ms << " ms (" << (double)input.size() / ((sort_ms + search_ms) / 1e3)
+            << " events/s end to end)" << std::endl;
+  return r;
 }
 
 void independent_post_execute(const std::vector<std::vector<uint8_t> >& output) {
