@@ -344,3 +344,18 @@ def test_device_budget_splits_large_batches(gpu_ctx, oracle_lib):
         assert gpu_ctx.stats().launches > 2                  # it was split
         for e in range(len(blobs)):
             assert index_lists(parts[e]) == index_lists(whole[e])
+
+
+def test_many_module_events_take_the_full_build(gpu_ctx, oracle_lib):
+    """Events with 64 or more modules run on the full shared-state build (the
+    compact one holds 63), alone and mixed with ordinary events, for every
+    register build and launch style."""
+    from cl_forward_gb300 import fuzz, generator
+    wide = [oracle_lib.sort_by_x(fuzz.fuzz_event(9000 + s, n_modules=n, max_per_module=10, grid=0.5, lines=8))
+            for s, n in enumerate((64, 80, 120, 255, 100, 70))]
+    mixed = wide + _sorted(oracle_lib, generator.generate(range(9100, 9110))[0])
+    for blobs in (wide, mixed):
+        for regs, threads in ((18, 64), (4, 128), (5, 256)):
+            for mode in (0, 1):
+                _assert_same(gpu_ctx, oracle_lib, blobs, register_ctas=regs, threads_per_event=threads,
+                             launch_mode=mode)
