@@ -573,10 +573,12 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
         best = key < best ? key : best;
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long other = __shfl_xor_sync(kFull, best, o);
-      best = other < best ? other : best;
+    {   // 64-bit minimum as two 32-bit warp reductions: the high words, then
+        // the low words of the lanes that hold the minimal high word
+      const uint32_t hi = (uint32_t)(best >> 32);
+      const uint32_t hmin = __reduce_min_sync(kFull, hi);
+      const uint32_t lmin = __reduce_min_sync(kFull, hi == hmin ? (uint32_t)best : 0xffffffffu);
+      best = ((unsigned long long)hmin << 32) | lmin;
     }
     if (lane == 0 && best != ~0ull) {   // Kernel.cl:550-567
       const uint32_t e = (uint32_t)(best >> 14) & 0x3fffu;
