@@ -79,11 +79,14 @@ VELO_HD ArenaLayout arena_layout(uint32_t H, uint32_t M, uint32_t Y) {
   (void)Y;
   ArenaLayout L;
   uint32_t o = 0;
-  L.x = o; o = align16(o + 4u * H);
-  L.y = o; o = align16(o + 4u * H);
-  L.z = o; o = align16(o + 4u * H);
-  L.win = o; o = align16(o + 8u * H);
-  L.used = o; o = align16(o + H);
+  // one stride P for every array, so a view of the arena is its base and P
+  const uint32_t P = align16(4u * H);
+  L.x = 0;
+  L.y = P;
+  L.z = 2u * P;
+  L.win = 3u * P;      // 8H bytes <= 2P
+  L.used = 5u * P;
+  o = 5u * P + align16(H);
   L.total = o;
   return L;
 }

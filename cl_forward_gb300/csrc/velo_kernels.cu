@@ -75,9 +75,15 @@ struct EventView {
   int S, H, Y;
   uint32_t cap;             // tracklet / track / weak rows (max(H, 1))
   uint32_t ring_cap;        // entries of each tracks-to-follow buffer (max(H, 1): one per seeded h0 at most)
-  float *x, *y, *z;
-  uint2* win;               // per hit: {h1 first | h1 last << 16, h2 first | h2 last << 16}
-  uint8_t* used;
+  // the arena: x, y, z, windows (per hit {h1 first | h1 last << 16, h2 first
+  // | h2 last << 16}) and used flags at multiples of one stride P
+  uint8_t* arena;
+  uint32_t P;
+  __device__ __forceinline__ float* xs() const { return reinterpret_cast<float*>(arena); }
+  __device__ __forceinline__ float* ys() const { return reinterpret_cast<float*>(arena + P); }
+  __device__ __forceinline__ float* zs() const { return reinterpret_cast<float*>(arena + 2u * P); }
+  __device__ __forceinline__ uint2* wins() const { return reinterpret_cast<uint2*>(arena + 3u * P); }
+  __device__ __forceinline__ uint8_t* useds() const { return arena + 5u * P; }
   uint4* ring0;             // tracks-to-follow buffers, selected by parity:
   uint4* ring1;             //   {entry word, first hit, previous hit, last hit}
   uint4* tracklets;         // {h0, h1, h2, 0} per tracklet
@@ -140,9 +146,9 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
   const int s2 = f - 2;
   const bool proc_h2 = f <= ev.S - 3;
   const int st2 = s.start[s2], n2 = s.num[s2];
-  const float x0 = ev.x[h], z0 = ev.z[h];
-  const float* x2 = ev.x + st2;
-  const float* z2 = ev.z + st2;
+  const float x0 = ev.xs()[h], z0 = ev.zs()[h];
+  const float* x2 = ev.xs() + st2;
+  const float* z2 = ev.zs() + st2;
   const bool sorted = ev.narrow && s.sorted[s2];
   uint32_t r1f = kNone16, r1l = kNone16, r2f = kNone16, r2l = kNone16;
 
@@ -224,7 +230,7 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
       if (found && r2l == kNone16) r2l = (uint32_t)n2;
     }
   }
-  ev.win[h] = make_uint2(r1f | (r1l << 16), r2f | (r2l << 16));
+  ev.wins()[h] = make_uint2(r1f | (r1l << 16), r2f | (r2l << 16));
 }
 
 // ---------------------------------------------------------------------------
@@ -287,16 +293,16 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
     trackno = full & kEntryNumber;
     const uint32_t n = is_tracklet ? 3u : (full >> kEntryCountShift) & 31u;
     const uint32_t h0 = en.z, h1 = en.w;   // the last two hits
-    const float h0x = ev.x[h0], h0y = ev.y[h0], h0z = ev.z[h0];
-    const float h1x = ev.x[h1], h1y = ev.y[h1], h1z = ev.z[h1];
+    const float h0x = ev.xs()[h0], h0y = ev.ys()[h0], h0z = ev.zs()[h0];
+    const float h1x = ev.xs()[h1], h1y = ev.ys()[h1], h1z = ev.zs()[h1];
     const float td = fdiv(1.0f, fsub(h1z, h0z));
     const float tx = fmul(fsub(h1x, h0x), td);
     const float ty = fmul(fsub(h1y, h0y), td);
 
     const int st4 = s.start[m4], n4 = s.num[m4];
-    const float* x4 = ev.x + st4;
-    const float* y4 = ev.y + st4;
-    const float* z4 = ev.z + st4;
+    const float* x4 = ev.xs() + st4;
+    const float* y4 = ev.ys() + st4;
+    const float* z4 = ev.zs() + st4;
     int lo = 0, hi = n4;
     if (ev.narrow && s.sorted[m4] && n4 > 0) {
       const float xa = fadd(h0x, fmul(tx, fsub(s.zmin[m4], h0z)));
@@ -334,11 +340,11 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
       if (n >= VELO_MAX_TRACK_SIZE) {   // the reference writes past hits[24] here
         atomicOr(&s.status, VELO_EVENT_TRACK_OVERFLOW);
       } else {
-        ev.used[best_h2] = 1;
+        ev.useds()[best_h2] = 1;
         if (is_tracklet) {   // third -> fourth hit: a track is allocated below; hits 0-2 marked
-          ev.used[en.y] = 1;
-          ev.used[en.z] = 1;
-          ev.used[en.w] = 1;
+          ev.useds()[en.y] = 1;
+          ev.useds()[en.z] = 1;
+          ev.useds()[en.w] = 1;
           action = kNewTrack;
         } else {
           velo_track& t = ev.tracks[trackno];
@@ -431,12 +437,12 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
   const int st1 = s.start[s1], st4 = s.start[m4], n4 = s.num[m4];
   const uint32_t Y = (uint32_t)ev.Y;
   const uint32_t chunk_step = 32u % Y;
-  const float s1_z = s.num[s1] > 0 ? ev.z[st1] : 0.f;   // Kernel.cl:420
+  const float s1_z = s.num[s1] > 0 ? ev.zs()[st1] : 0.f;   // Kernel.cl:420
   const bool narrow4 = ev.narrow && s.sorted[m4] && n4 > 0;
   const float zmin4 = s.zmin[m4], zmax4 = s.zmax[m4];
-  const float* x4 = ev.x + st4;
-  const float* y4 = ev.y + st4;
-  const float* z4 = ev.z + st4;
+  const float* x4 = ev.xs() + st4;
+  const float* y4 = ev.ys() + st4;
+  const float* z4 = ev.zs() + st4;
   bool degenerate = false;
   // 1 / (z1 - z0) by bit patterns of (z0, z1): hits of a module share few z
   // values, so the division is rarely redone (same operands, same result)
@@ -445,12 +451,12 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
 
   for (int i = warp; i < n0; i += nwarps) {
     const int h0 = st0 + i;
-    if (ev.used[h0]) continue;                       // warp-uniform
-    const uint32_t w0 = ev.win[h0].x;
+    if (ev.useds()[h0]) continue;                       // warp-uniform
+    const uint32_t w0 = ev.wins()[h0].x;
     const uint32_t f1 = w0 & 0xffffu;
     if (f1 == kNone16) continue;
     const int n1 = (int)(w0 >> 16) - (int)f1;        // > 0 when a first hit was found
-    const float h0x = ev.x[h0], h0y = ev.y[h0], h0z = ev.z[h0];
+    const float h0x = ev.xs()[h0], h0y = ev.ys()[h0], h0z = ev.zs()[h0];
     const float dymax = fmul(kMaxYSlope, fabsf(fsub(s1_z, h0z)));
     H0Features g0{};
     if constexpr (kMode != kPlain) g0 = h0_features(h0x, h0y, f, ev.S, dymax);
@@ -464,19 +470,19 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
       if (ly >= Y) ly -= Y;
       const int h1 = st1 + (int)f1 + e;
       uint32_t w1 = 0;
-      if (in) w1 = ev.win[h1].y;
+      if (in) w1 = ev.wins()[h1].y;
       const bool dead = in && (w1 & 0xffffu) == kNone16;
       const unsigned dmask = __ballot_sync(kFull, dead);
       const bool stopped = ((dmask & below_same_lane) != 0) || ((dead_lanes >> ly) & 1u);
       dead_lanes |= __reduce_or_sync(kFull, dead ? (1u << ly) : 0u);
       chunk_mod += chunk_step;
       if (chunk_mod >= Y) chunk_mod -= Y;
-      bool cand = in && !dead && !stopped && !ev.used[h1];
+      bool cand = in && !dead && !stopped && !ev.useds()[h1];
       float h1x = 0.f, h1y = 0.f, h1z = 0.f;
       if (cand) {
-        h1x = ev.x[h1];
-        h1y = ev.y[h1];
-        h1z = ev.z[h1];
+        h1x = ev.xs()[h1];
+        h1y = ev.ys()[h1];
+        h1z = ev.zs()[h1];
         cand = fabsf(fsub(h1y, h0y)) < dymax;        // h2-independent term of Kernel.cl:509
       }
       int a = (int)(w1 & 0xffffu), b = (int)(w1 >> 16);
@@ -651,11 +657,8 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
 
   const ArenaLayout L = arena_layout((uint32_t)H, p.ev_maxmod[e], (uint32_t)ev.Y);
   uint8_t* arena = p.arena_off[e] == kNoArena ? dyn : p.global_arena + p.arena_off[e];
-  ev.x = reinterpret_cast<float*>(arena + L.x);
-  ev.y = reinterpret_cast<float*>(arena + L.y);
-  ev.z = reinterpret_cast<float*>(arena + L.z);
-  ev.win = reinterpret_cast<uint2*>(arena + L.win);
-  ev.used = arena + L.used;
+  ev.arena = arena;
+  ev.P = L.y;
   const uint64_t hb = p.hit_base[e];
   ev.ring0 = reinterpret_cast<uint4*>(p.rings + 8 * hb);
   ev.ring1 = ev.ring0 + ev.cap;
@@ -687,10 +690,10 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   for (int i = tid; i < H; i += nt) {
     const float xv = gx[i], yv = gy[i], zv = gz[i];
     bad |= !(isfinite(xv) && isfinite(yv) && isfinite(zv));
-    ev.x[i] = xv;
-    ev.y[i] = yv;
-    ev.z[i] = zv;
-    ev.used[i] = 0;
+    ev.xs()[i] = xv;
+    ev.ys()[i] = yv;
+    ev.zs()[i] = zv;
+    ev.useds()[i] = 0;
   }
   if (tid == 0) {
     s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
@@ -713,10 +716,10 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     float zmn = FLT_MAX, zmx = -FLT_MAX;
     bool sorted = true;
     for (int i = lane; i < n; i += 32) {
-      const float z = ev.z[st + i];
+      const float z = ev.zs()[st + i];
       zmn = fminf(zmn, z);
       zmx = fmaxf(zmx, z);
-      if (i + 1 < n && !(ev.x[st + i] <= ev.x[st + i + 1])) sorted = false;
+      if (i + 1 < n && !(ev.xs()[st + i] <= ev.xs()[st + i + 1])) sorted = false;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -732,7 +735,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   }
   // windows of modules 0..3 stay empty (Kernel.cl:104 gates the body on f >= 4)
   const int hbeg = S >= 5 ? s.start[4] : H;
-  for (int i = tid; i < hbeg; i += nt) ev.win[i] = make_uint2(0xffffffffu, 0xffffffffu);
+  for (int i = tid; i < hbeg; i += nt) ev.wins()[i] = make_uint2(0xffffffffu, 0xffffffffu);
   __syncthreads();
   VELO_PHASE(1);
 
@@ -762,7 +765,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   uint32_t fallback = (kMode == kLearned && !learned) ? VELO_EVENT_LEARNED_FALLBACK : 0u;
   for (int attempt = 0; attempt < 2; ++attempt) {
     if (attempt > 0) {
-      for (int i = tid; i < H; i += nt) ev.used[i] = 0;
+      for (int i = tid; i < H; i += nt) ev.useds()[i] = 0;
       if (tid == 0) {
         s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
         s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
@@ -815,7 +818,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       for (uint32_t i = tid; i < nweak; i += nt) {
         const uint4 t = ev.tracklets[ev.weak[i]];
         const uint32_t a = t.x, bb = t.y, c = t.z;
-        if (!ev.used[a] && !ev.used[bb] && !ev.used[c]) {
+        if (!ev.useds()[a] && !ev.useds()[bb] && !ev.useds()[c]) {
           const uint32_t tn = atomicAdd(&s.ntracks, 1u);
           if (tn >= ev.cap) continue;
           uint32_t* wr = reinterpret_cast<uint32_t*>(&ev.tracks[tn]);
