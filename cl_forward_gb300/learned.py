@@ -1,6 +1,6 @@
 """Learned doublet pruning: training data, training, calibration, evaluation.
 
-The plain method is both the teacher and the judge:
+The plain method is both the teacher and the yardstick:
 
 * training data -- the search kernel records the features of the doublets that
   reach the h2 search during a plain run (``velo_dump_doublets``, so training
