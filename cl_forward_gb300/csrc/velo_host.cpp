@@ -26,6 +26,7 @@ namespace {
 int g_verbosity = 0;   // 3 in standalone mode, 0 in framework mode (GpuPixelSearchByTriplet.cpp:16,35)
 velo_ctx* g_ctx = nullptr;
 std::mutex g_mutex;
+std::mutex g_call_mutex;   // one search at a time on the shared context (the reference is not re-entrant)
 // pinned track buffer the kernel writes in place, kept between calls
 velo_track* g_tracks = nullptr;
 uint64_t g_tracks_cap = 0;
@@ -73,6 +74,7 @@ int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
                          std::vector<std::vector<uint8_t> >& output) {
   if (eventsToProcess <= 0) return 0;
   velo_ctx* c = context();
+  std::lock_guard<std::mutex> call_lock(g_call_mutex);
   std::vector<const uint8_t*> ptrs(eventsToProcess);
   std::vector<uint64_t> sizes(eventsToProcess);
   for (int i = 0; i < eventsToProcess; ++i) {
