@@ -248,6 +248,14 @@ class Context:
                     "velo_fetch")
         return tracks, counts[:n_events], first[:n_events], status[:n_events]
 
+    def fetch_counts(self, n_events: int):
+        """Per-event counts, first rows and status of the last run, without the tracks."""
+        counts = np.zeros(max(n_events, 1), np.uint32)
+        first = np.zeros(max(n_events, 1), np.uint64)
+        status = np.zeros(max(n_events, 1), np.uint32)
+        self._check(self._lib.velo_fetch(self._h, None, 0, _p(counts), _p(first), _p(status)), "velo_fetch")
+        return counts[:n_events], first[:n_events], status[:n_events]
+
     def fetch_into(self, tracks: np.ndarray, counts: np.ndarray, first: np.ndarray, status: np.ndarray):
         self._check(self._lib.velo_fetch(self._h, _p(tracks), len(tracks), _p(counts), _p(first),
                                          _p(status)), "velo_fetch")
