@@ -143,7 +143,18 @@ def make_workload(args, rank: int):
 
 
 def sort_events(raw):
-    from oracle import oracle   # sort only: the reference's preorder_by_x, restated
+    """The library's host x-sort (velo_sort_by_x: the reference's preorder_by_x
+    permutation), on the host's cores; pure host code, no CUDA context."""
+    from concurrent.futures import ThreadPoolExecutor
+    from cl_forward_gb300 import build, native
+    build.build()
+    native.load()
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(native.sort_by_x, raw))
+
+
+def sort_events_reference(raw):
+    from oracle import oracle   # the reference arm sorts with the reference's sort, restated
     return [oracle.sort_by_x(b) for b in raw]
 
 
@@ -253,7 +264,7 @@ def reference_arm(args, ranks: Ranks):
     if ranks.rank != 0:
         return None
     raw, _ = make_workload(args, 0)
-    blobs = sort_events(raw)
+    blobs = sort_events_reference(raw)
     from oracle import oracle
     n = len(blobs)
     kind = "port"
