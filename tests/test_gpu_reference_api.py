@@ -64,6 +64,8 @@ def test_cpp_driver_dump(native_lib, oracle_lib, tmp_path):
         ev = events.unpack_event(oracle_lib.sort_by_x(raw[i]))
         ref_ids = sorted(tuple(sorted(int(ev.hit_id[h]) for h in t)) for t in index_lists(want[i]))
         assert ids == ref_ids
+        from cl_forward_gb300 import compare                 # the dump reader sees the same tracks
+        assert sorted(tuple(sorted(t)) for t in compare.read_dump(str(dump / f"{i}.out"))) == ref_ids
 
 
 def test_cpp_driver_sorts_many_events_in_parallel(native_lib, oracle_lib, tmp_path):
