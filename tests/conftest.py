@@ -9,7 +9,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "golden_tracks.npz")
-GOLDEN_SETS = ("velo", "fuzz", "edge")
+GOLDEN_SETS = ("velo", "fuzz", "mcdata", "edge")
 GOLDEN_Y = (1, 2, 4)
 
 

@@ -6,7 +6,9 @@ reference's preorder_by_x (Tools.cpp:46-66) and the tracks are the
 reference's clSearchByTriplets (Kernel.cl:597-816) run under the work-group
 emulator (oracle/ref_emu.c), at local size (64, Y).  Inputs are seeded
 synthetic events (cl_forward_gb300.generator / .fuzz), stored as bytes so the
-fixture does not depend on the generator staying bit-identical.
+fixture does not depend on the generator staying bit-identical, and the
+first six real events of the reference's mcdata/ (real geometry: several z
+values per module, unsorted hits).
 
 Run in a checkout next to the reference sources:
     python tests/golden/make_golden.py [--reference DIR]
@@ -23,8 +25,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from cl_forward_gb300 import fuzz, generator  # noqa: E402
-from oracle import oracle  # noqa: E402
+from cl_forward_gb300 import events, fuzz, generator  # noqa: E402
+from oracle import build_ref, oracle  # noqa: E402
 
 OUT = os.path.join(HERE, "golden_tracks.npz")
 Y_VALUES = (1, 2, 4)
@@ -58,6 +60,8 @@ def main():
                  for s in (0, 3, 7, 11, 19, 23, 42, 57)]
                 + [fuzz.fuzz_event(2000 + s, jitter_z=True) for s in range(4)]
                 + [fuzz.fuzz_event(s, grid=2.0) for s in range(4)],
+        "mcdata": [events.read_dat(os.path.join(build_ref.default_reference(), "mcdata", f"{i}.dat"))
+                   for i in range(6)],
         "edge": [fuzz.empty_event(), fuzz.empty_event(0), fuzz.empty_event(4),
                  fuzz.fuzz_event(3000, n_modules=5), fuzz.fuzz_event(3001, n_modules=7),
                  fuzz.fuzz_event(3002, max_per_module=1, lines=1)],

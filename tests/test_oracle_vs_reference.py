@@ -71,3 +71,37 @@ def test_overflow_flags(oracle_lib):
     blobs = [oracle_lib.sort_by_x(fuzz.fuzz_event(s, lines=12, max_per_module=2)) for s in range(40)]
     _, status = oracle_lib.search(blobs, 4)
     assert np.any(status & oracle_lib.EVENT_TRACK_OVERFLOW)
+
+
+def test_predecessor_tracks_in_mcdata_are_found(oracle_lib):
+    """Each mcdata file carries, after the event, the tracks of a predecessor
+    producer (records {4-word header, hitsNum, hits[24]}, hit indices in the
+    file's unsorted order).  They are not this kernel's output, but the same
+    physics: the restatement (pinned to the reference kernel) reproduces at
+    least 95 % of them exactly as sets of hit IDs (measured: 96.0 %)."""
+    import struct
+    from cl_forward_gb300 import events
+    mc = os.path.join(ref_dir, "mcdata")
+    if not os.path.isdir(mc):
+        pytest.skip("reference mcdata not available")
+    total = exact = 0
+    for name in sorted(os.listdir(mc), key=lambda f: int(f.split(".")[0])):
+        data = open(os.path.join(mc, name), "rb").read()
+        (nl,) = struct.unpack_from("<i", data, 0)
+        o = 4 + nl
+        (size,) = struct.unpack_from("<i", data, o)
+        blob = data[o + 4:o + 4 + size]
+        o += 4 + size
+        (nbytes,) = struct.unpack_from("<i", data, o)
+        rec = np.frombuffer(data, np.uint32, nbytes // 4, o + 4).reshape(-1, 29)
+        ev = events.unpack_event(blob)
+        sb = oracle_lib.sort_by_x(blob)
+        evs = events.unpack_event(sb)
+        tracks, _ = oracle_lib.search([sb], 4)
+        mine = {frozenset(int(evs.hit_id[h]) for h in t["hits"][:int(t["hitsNum"])]) for t in tracks[0]}
+        for r in rec:
+            n = int(r[4])
+            if n >= 3 and np.all(r[5:5 + n] < len(ev.hit_id)):
+                total += 1
+                exact += frozenset(int(ev.hit_id[h]) for h in r[5:5 + n]) in mine
+    assert total > 15000 and exact >= 0.95 * total
