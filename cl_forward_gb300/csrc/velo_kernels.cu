@@ -3,9 +3,13 @@
 // One CTA reconstructs one event (the reference's one work-group per event,
 // Kernel.cl:607, KernelInvoker.cpp:26-27), either one CTA per event or
 // persistent CTAs pulling events, largest first, from a work queue.  The
-// event's hits and its per-hit working state live in dynamic shared memory
-// (the "arena"); events too large for the launch's arena use a global-memory
-// arena with the same layout.
+// event's hits and its per-hit working state (the "arena": x, y, z,
+// candidate windows, used flags) live in dynamic shared memory when the event
+// fits the launch's tile, else in global scratch with the same layout, which
+// L1 caches.  On GB300 the fastest launch keeps the tile tiny: shared memory
+// and L1 share each SM's storage, and resident CTAs are register-bound, so L1
+// serves the arenas better than staging does.  The tracks-to-follow rings,
+// tracklets and working tracks are per-hit-row global scratch.
 //
 // Decisions are the reference's, bit for bit:
 //  * every FP32 expression is written with round-to-nearest intrinsics
