@@ -359,3 +359,32 @@ def test_many_module_events_take_the_full_build(gpu_ctx, oracle_lib):
             for mode in (0, 1):
                 _assert_same(gpu_ctx, oracle_lib, blobs, register_ctas=regs, threads_per_event=threads,
                              launch_mode=mode)
+
+
+def test_contexts_in_concurrent_threads(gpu_ctx, oracle_lib):
+    """One context per host thread: four threads searching different batches
+    at the same time (the library's calls release the interpreter) get the
+    tracks a single thread gets."""
+    import threading
+    from cl_forward_gb300 import generator, native
+    batches = [_sorted(oracle_lib, generator.generate(range(9500 + 100 * k, 9560 + 100 * k))[0]) for k in range(4)]
+    want = [gpu_ctx.search(b)[0] for b in batches]
+    got = [None] * 4
+    errors = []
+
+    def work(k):
+        try:
+            with native.Context(0) as ctx:
+                for _ in range(3):
+                    got[k] = ctx.search(batches[k], native.default_options(host_direct=k % 2))[0]
+        except Exception as exc:   # reported below, on the main thread
+            errors.append(exc)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for k in range(4):
+        assert [index_lists(t) for t in got[k]] == [index_lists(t) for t in want[k]]
