@@ -36,6 +36,17 @@ def test_velo_events(ref):
     assert n == 40 and not bad
 
 
+def test_schedule_seeds_agree(ref):
+    """The reference kernel's track contents do not depend on the order in
+    which its work-items run between barriers: the in-order schedule and five
+    seeded random schedules all give the restatement's tracks."""
+    from cl_forward_gb300 import generator
+    blobs, _ = generator.generate(range(1000, 1030))
+    for seed in range(6):
+        bad, n = _compare(ref, blobs, 4, seed)
+        assert n == 30 and not bad, (seed, bad)
+
+
 @pytest.mark.parametrize("y", [1, 3, 4, 16])
 def test_fuzz_events(ref, y):
     from cl_forward_gb300 import fuzz
