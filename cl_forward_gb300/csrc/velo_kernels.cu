@@ -240,7 +240,7 @@ __device__ void compute_windows(const EventView& ev, const Shared& s, int h, int
 // ---------------------------------------------------------------------------
 // Tracks-to-follow entries.  Bit 31 marks a tracklet (3 hits, number = its
 // row in the tracklet list) and bits 28-30 count skipped modules, as in the
-// reference (Kernel.cl:222-225,351,566).  This build also keeps a track's
+// reference (Kernel.cl:222-225,351,566).  This kernel also keeps a track's
 // hit count in bits 23-27 (the reference re-reads it from the track), so
 // numbers use bits 0-22.
 constexpr uint32_t kEntryNumber = 0x007FFFFFu;
