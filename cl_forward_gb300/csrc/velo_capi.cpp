@@ -2,9 +2,11 @@
 //
 // Replaces invokeParallelSearch (KernelInvoker.cpp:14-275): instead of a fresh
 // OpenCL context, a JIT build and twelve buffers per call, a velo_ctx keeps
-// one CUDA stream and grow-only device buffers; events are validated on the
-// host (headers and module tables), copied with one H2D transfer, searched by
-// one kernel launch, and the tracks come back compacted in one D2H transfer.
+// one CUDA stream and grow-only device buffers; event headers are checked on
+// the host (module tables and coordinates by the search kernel), the events
+// are copied with one H2D transfer (or read in place from mapped pinned host
+// memory), searched by one kernel launch, and the tracks come back compacted
+// in one D2H transfer (or are written in place).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -448,6 +450,10 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   for (int32_t e = 0; e < n; ++e) {
     if (offsets[e] & 3u) {
       c->err = "event offsets must be 4-byte aligned";
+      return VELO_ERR_INVALID_ARGUMENT;
+    }
+    if (sizes[e] > ~0ull - offsets[e]) {
+      c->err = "event offset + size overflows";
       return VELO_ERR_INVALID_ARGUMENT;
     }
     lo = std::min(lo, offsets[e]);

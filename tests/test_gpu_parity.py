@@ -199,6 +199,14 @@ def test_edge_cases(gpu_ctx, oracle_lib):
         gpu_ctx.search(batch)                                  # strict call reports the bad events
     out, st = gpu_ctx.search([])
     assert out == [] and len(st) == 0
+    # batch descriptions that are rejected before anything is copied
+    for offs, sizes in (([2], [len(good[0])]),                       # offset not 4-byte aligned
+                        ([8], [np.iinfo(np.uint64).max - 4])):        # offset + size wraps around
+        with pytest.raises(native.VeloError) as err:
+            gpu_ctx.stage(pbuf, np.array(offs, np.uint64), np.array(sizes, np.uint64))
+        assert err.value.status == native.ERR_INVALID_ARGUMENT
+    got, _ = gpu_ctx.search([good[0]])                                 # the context still works
+    assert index_lists(got[0]) == index_lists(want[0])
 
 
 def test_context_reuse_is_stable(gpu_ctx, oracle_lib):
