@@ -71,3 +71,31 @@ def empty_event(n_modules: int = N_MODULES) -> bytes:
                np.zeros(0, np.uint32), np.zeros(0, np.float32), np.zeros(0, np.float32),
                np.zeros(0, np.float32))
     return pack_event(ev)
+
+
+def crowded_event(seed: int, n_hits: int, module: int = 20, base_seed: int = 9500) -> bytes:
+    """A fuzz event whose module `module` holds `n_hits` uniformly spread hits
+    (on a 0.05 mm grid, x and y in [-40, 40] mm) in place of its own: the
+    occupancy limit of one module (VELO_MAX_MODULE_HITS) and one past it."""
+    from .events import unpack_event
+    base = unpack_event(fuzz_event(base_seed, max_per_module=8, grid=0.5, lines=8))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    S = base.n_sensors
+    mod_of = base.module_of_hit()
+    keep = mod_of != module
+    new_x = np.round(rng.uniform(-40, 40, n_hits) / 0.05) * 0.05
+    new_y = np.round(rng.uniform(-40, 40, n_hits) / 0.05) * 0.05
+    mods = np.concatenate([mod_of[keep], np.full(n_hits, module)])
+    xs = np.concatenate([base.x[keep], new_x.astype(np.float32)])
+    ys = np.concatenate([base.y[keep], new_y.astype(np.float32)])
+    zs = np.concatenate([base.z[keep], np.full(n_hits, MODULE_Z[module], np.float32)])
+    order = np.argsort(mods, kind="stable")
+    mods = mods[order]
+    counts = np.bincount(mods, minlength=S).astype(np.int32)
+    starts = np.zeros(S, np.int32)
+    starts[1:] = np.cumsum(counts)[:-1]
+    H = len(mods)
+    ev = Event(sensor_z=base.sensor_z.copy(), hit_start=starts, hit_num=counts,
+               hit_id=((np.arange(H, dtype=np.uint64) + 1) << np.uint64(8) | mods.astype(np.uint64)).astype(np.uint32),
+               x=xs[order].astype(np.float32), y=ys[order].astype(np.float32), z=zs[order].astype(np.float32))
+    return pack_event(ev)

@@ -369,6 +369,26 @@ def test_many_module_events_take_the_full_build(gpu_ctx, oracle_lib):
                              launch_mode=mode)
 
 
+def test_maximum_module_occupancy(gpu_ctx, oracle_lib):
+    """Modules holding the most hits a module may hold (16,383): on modules 38
+    and 39 (50 mm from the h0 modules above them) an h0's h1 window spans
+    ~14,000 hits, near the top of the seeding key's 14-bit element field.
+    Every launch style gives the oracle's tracks; a module of one hit more
+    makes its event invalid and leaves the rest of the batch alone."""
+    from cl_forward_gb300 import fuzz, native
+    full = [oracle_lib.sort_by_x(fuzz.crowded_event(s, 16383, module=m)) for s, m in ((1, 38), (2, 39), (3, 20))]
+    for regs, threads in ((18, 64), (5, 256)):
+        for mode in (0, 1):
+            _, checked = _assert_same(gpu_ctx, oracle_lib, full, register_ctas=regs, threads_per_event=threads,
+                                      launch_mode=mode)
+            assert checked == 3
+    over = fuzz.crowded_event(1, 16384, module=38)
+    got, status = gpu_ctx.search([full[0], over, full[2]], allow_invalid=True)
+    want, _ = oracle_lib.search([full[0], full[2]], 4)
+    assert status[1] & native.EVENT_INVALID and len(got[1]) == 0
+    assert index_lists(got[0]) == index_lists(want[0]) and index_lists(got[2]) == index_lists(want[1])
+
+
 def test_contexts_in_concurrent_threads(gpu_ctx, oracle_lib):
     """One context per host thread: four threads searching different batches
     at the same time (the library's calls release the interpreter) get the

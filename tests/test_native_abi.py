@@ -69,6 +69,9 @@ def test_validate_event(native_lib):
     bad = bytearray(events.pack_event(ev))
     bad[0:4] = (300).to_bytes(4, "little")                                 # too many modules
     assert native.validate_event(bytes(bad)) == native.ERR_INVALID_EVENT
+    from cl_forward_gb300 import fuzz                                      # module occupancy limit
+    assert native.validate_event(fuzz.crowded_event(1, 16383)) == native.OK
+    assert native.validate_event(fuzz.crowded_event(1, 16384)) == native.ERR_INVALID_EVENT
 
 
 def test_native_sort_matches_oracle_sort(native_lib, oracle_lib, golden):
