@@ -116,17 +116,19 @@ __device__ __forceinline__ int first_gt(const float* x, int lo, int hi, float c)
 // Sub-range [lo, hi) of [lo0, hi0) on a sorted module outside which no hit
 // can satisfy |fl(xp - x)| < tol for any predicted xp in [xl, xh].  The upper
 // end is usually a few hits past the lower one: walk, then bisect.
-__device__ __forceinline__ void narrow_range(const float* x, int lo0, int hi0, float xl, float xh, float tol,
-                                             int* lo, int* hi) {
+// x_first = x[lo0] and x_last = x[hi0 - 1] are passed in (any value when
+// lo0 == hi0), so that a caller can load them early.
+__device__ __forceinline__ void narrow_range_ends(const float* x, int lo0, int hi0, float x_first, float x_last,
+                                                  float xl, float xh, float tol, int* lo, int* hi) {
   const float margin = fadd(0.01f, fmul(1e-5f, fadd(fabsf(xl), fabsf(xh))));
   const float lt = fsub(fsub(xl, tol), margin);
   const float ht = fadd(fadd(xh, tol), margin);
   if (isfinite(lt) && isfinite(ht)) {
-    // both ends first (two independent loads): a prediction beyond either end
-    // of the module (a track tried on the other detector half) is settled
-    // without the bisection, with the bisection's own result
-    if (lo0 < hi0 && (x[hi0 - 1] <= lt || x[lo0] > ht)) {
-      *lo = *hi = x[lo0] > ht ? lo0 : hi0;
+    // both ends first: a prediction beyond either end of the module (a track
+    // tried on the other detector half) is settled without the bisection,
+    // with the bisection's own result
+    if (lo0 < hi0 && (x_last <= lt || x_first > ht)) {
+      *lo = *hi = x_first > ht ? lo0 : hi0;
       return;
     }
     const int l = first_gt(x, lo0, hi0, lt);
@@ -140,6 +142,16 @@ __device__ __forceinline__ void narrow_range(const float* x, int lo0, int hi0, f
     *lo = lo0;
     *hi = hi0;
   }
+}
+
+__device__ __forceinline__ void narrow_range(const float* x, int lo0, int hi0, float xl, float xh, float tol,
+                                             int* lo, int* hi) {
+  float x_first = 0.f, x_last = 0.f;
+  if (lo0 < hi0) {   // two independent loads
+    x_first = x[lo0];
+    x_last = x[hi0 - 1];
+  }
+  narrow_range_ends(x, lo0, hi0, x_first, x_last, xl, xh, tol, lo, hi);
 }
 
 // ---------------------------------------------------------------------------
@@ -289,6 +301,15 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
   int action = kNone;
   uint32_t push_value = 0, trackno = 0, best_h2 = 0;
   uint4 en = make_uint4(0, 0, 0, 0);
+  // the ends of module m4 for the narrowing, loaded alongside the entry
+  // (same addresses in every lane)
+  const int st4 = s.start[m4], n4 = s.num[m4];
+  const float* x4 = ev.xs() + st4;
+  float x4_first = 0.f, x4_last = 0.f;
+  if (n4 > 0) {
+    x4_first = x4[0];
+    x4_last = x4[n4 - 1];
+  }
   if (i < ncur) {
     en = ring_entry(ev, b, lo_n, i);
     const uint32_t full = en.x;
@@ -303,15 +324,14 @@ __device__ void forward_warp(const EventView& ev, Shared& s, int b, uint32_t lo_
     const float tx = fmul(fsub(h1x, h0x), td);
     const float ty = fmul(fsub(h1y, h0y), td);
 
-    const int st4 = s.start[m4], n4 = s.num[m4];
-    const float* x4 = ev.xs() + st4;
     const float* y4 = ev.ys() + st4;
     const float* z4 = ev.zs() + st4;
     int lo = 0, hi = n4;
     if (ev.narrow && s.sorted[m4] && n4 > 0) {
       const float xa = fadd(h0x, fmul(tx, fsub(s.zmin[m4], h0z)));
       const float xb = fadd(h0x, fmul(tx, fsub(s.zmax[m4], h0z)));
-      if (isfinite(xa) && isfinite(xb)) narrow_range(x4, 0, n4, fminf(xa, xb), fmaxf(xa, xb), kTolerance, &lo, &hi);
+      if (isfinite(xa) && isfinite(xb))
+        narrow_range_ends(x4, 0, n4, x4_first, x4_last, fminf(xa, xb), fmaxf(xa, xb), kTolerance, &lo, &hi);
     }
     // fitHitToTrack (Kernel.cl:15-35) over the candidates, first minimum wins.
     // The scatter's 1/(z2 - z1) depends only on z2 here: it is recomputed only
@@ -473,22 +493,25 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
       uint32_t ly = lane_mod + chunk_mod;
       if (ly >= Y) ly -= Y;
       const int h1 = st1 + (int)f1 + e;
+      // everything the cuts read about h1, loaded at once (one round trip)
       uint32_t w1 = 0;
-      if (in) w1 = ev.wins()[h1].y;
+      uint8_t u1 = 1;
+      float h1x = 0.f, h1y = 0.f, h1z = 0.f;
+      if (in) {
+        w1 = ev.wins()[h1].y;
+        u1 = ev.useds()[h1];
+        h1x = ev.xs()[h1];
+        h1y = ev.ys()[h1];
+        h1z = ev.zs()[h1];
+      }
       const bool dead = in && (w1 & 0xffffu) == kNone16;
       const unsigned dmask = __ballot_sync(kFull, dead);
       const bool stopped = ((dmask & below_same_lane) != 0) || ((dead_lanes >> ly) & 1u);
       dead_lanes |= __reduce_or_sync(kFull, dead ? (1u << ly) : 0u);
       chunk_mod += chunk_step;
       if (chunk_mod >= Y) chunk_mod -= Y;
-      bool cand = in && !dead && !stopped && !ev.useds()[h1];
-      float h1x = 0.f, h1y = 0.f, h1z = 0.f;
-      if (cand) {
-        h1x = ev.xs()[h1];
-        h1y = ev.ys()[h1];
-        h1z = ev.zs()[h1];
-        cand = fabsf(fsub(h1y, h0y)) < dymax;        // h2-independent term of Kernel.cl:509
-      }
+      bool cand = in && !dead && !stopped && !u1;
+      if (cand) cand = fabsf(fsub(h1y, h0y)) < dymax;   // h2-independent term of Kernel.cl:509
       int a = (int)(w1 & 0xffffu), b = (int)(w1 >> 16);
       float tol = kTolerance;
       float dz_inverted = 0.f;
