@@ -538,8 +538,8 @@ def gpu_arm(args, ranks: Ranks):
                      "algorithmic_bytes": alg_bytes, "peak_source": peak_src,
                      "note": "algorithmic bytes = input blobs + 4 B count + 100 B per track",
                      "limiter": ("not HBM: a latency- and issue-bound search (the ncu capture in "
-                                 "traffic_source: ~58% of issue slots busy, DRAM ~3%, L2 ~8%, L1 hit rate "
-                                 "~89%)")},
+                                 "traffic_source: ~60% of issue slots busy, DRAM ~3%, L2 ~6%, L1 hit rate "
+                                 "~87%)")},
         "clocks": clk.summary(),
         "gpu_launches": launches,
         "status_flags": {"ring_overflow": int(np.sum(status & 1 != 0)),
