@@ -16,6 +16,7 @@
 #include <chrono>
 #include <mutex>
 #include <thread>
+#include <string>
 #include <vector>
 
 #include "../../include/GpuPixelSearchByTriplet.h"
@@ -30,6 +31,9 @@ std::mutex g_call_mutex;   // one search at a time on the shared context (the re
 // pinned track buffer the kernel writes in place, kept between calls
 velo_track* g_tracks = nullptr;
 uint64_t g_tracks_cap = 0;
+// pinned buffer independent_execute gathers the events into
+uint8_t* g_gather = nullptr;
+uint64_t g_gather_cap = 0;
 
 // Runs f(a, b) over [0, n) on the host's cores when n is large.
 template <class F>
@@ -67,6 +71,76 @@ velo_ctx* context() {
   return g_ctx;
 }
 
+// Grow-only pinned buffer of at least `bytes` (not zero-filled).
+template <typename T>
+T* pinned(velo_ctx* c, T*& buf, uint64_t& cap, uint64_t count, const char* where) {
+  if (count > cap) {
+    if (buf) velo_host_free(c, buf);
+    buf = nullptr;
+    cap = 0;
+    void* p = nullptr;
+    const uint64_t want = count + count / 4;
+    velo_status st = velo_host_alloc(c, want * sizeof(T), &p);
+    if (st != VELO_OK) fail(where, st, velo_last_error(c));
+    buf = static_cast<T*>(p);
+    cap = want;
+  }
+  return buf;
+}
+
+// independent_execute's sort and search of input[a, a + n) on the GPU: the
+// events are gathered into pinned memory, copied to the device, sorted there
+// with the reference's permutation (velo_sort_staged, byte for byte the
+// result of preorder_by_x), searched, and the sorted bytes are written back
+// into the caller's buffers, which the reference sorts in place through
+// const pointers (Tools.cpp:51-63).
+void sort_and_search(const std::vector<const std::vector<uint8_t>*>& input, int a, int n,
+                     std::vector<std::vector<uint8_t> >& output) {
+  if (n <= 0) return;
+  velo_ctx* c = context();
+  std::lock_guard<std::mutex> call_lock(g_call_mutex);
+  std::vector<const uint8_t*> ptrs(n);
+  std::vector<uint64_t> offs(n), sizes(n);
+  uint64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    const std::vector<uint8_t>* v = input[a + i];
+    ptrs[i] = v->empty() ? nullptr : v->data();
+    sizes[i] = v->size();
+    offs[i] = total;
+    total += (sizes[i] + 15u) & ~15ull;
+  }
+  uint8_t* buf = pinned(c, g_gather, g_gather_cap, total ? total : 16, "independent_execute");
+  parallel_for((size_t)n, 256, [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; ++i)
+      if (sizes[i]) std::memcpy(buf + offs[i], ptrs[i], sizes[i]);
+  });
+  const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), n);
+  velo_track* tracks = pinned(c, g_tracks, g_tracks_cap, cap, "independent_execute");
+  std::vector<uint32_t> counts(n), status(n);
+  std::vector<uint64_t> first(n);
+  velo_options opts;
+  velo_default_options(&opts);   // Y = 4, the reference's output configuration
+  velo_status st = velo_stage(c, buf, offs.data(), sizes.data(), n);
+  if (st == VELO_OK) st = velo_sort_staged(c);
+  if (st == VELO_OK) st = velo_run(c, &opts);
+  if (st == VELO_OK) st = velo_fetch(c, tracks, g_tracks_cap, counts.data(), first.data(), status.data());
+  if (st == VELO_OK) st = velo_fetch_staged(c, buf, total);
+  if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
+  for (int i = 0; i < n; ++i)
+    if (status[i] & VELO_EVENT_INVALID) {
+      const std::string what = "event " + std::to_string(a + i) + " failed validation";
+      fail("invokeParallelSearch", VELO_ERR_INVALID_EVENT, what.c_str());
+    }
+  parallel_for((size_t)n, 256, [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; ++i) {
+      if (sizes[i]) std::memcpy(const_cast<uint8_t*>(ptrs[i]), buf + offs[i], sizes[i]);
+      std::vector<uint8_t>& out = output[a + i];
+      out.resize((size_t)counts[i] * sizeof(velo_track));
+      if (counts[i]) std::memcpy(out.data(), &tracks[first[i]], out.size());
+    }
+  });
+}
+
 }  // namespace
 
 int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
@@ -82,19 +156,9 @@ int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
     ptrs[i] = v->empty() ? nullptr : v->data();
     sizes[i] = v->size();
   }
+  // grow-only, not zero-filled: only [first, first + count) is read
   const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), eventsToProcess);
-  if (cap > g_tracks_cap) {   // grow-only, not zero-filled: only [first, first + count) is read
-    if (g_tracks) velo_host_free(c, g_tracks);
-    g_tracks = nullptr;
-    g_tracks_cap = 0;
-    void* p = nullptr;
-    const uint64_t want = cap + cap / 4;
-    velo_status st = velo_host_alloc(c, want * sizeof(velo_track), &p);
-    if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
-    g_tracks = static_cast<velo_track*>(p);
-    g_tracks_cap = want;
-  }
-  velo_track* tracks = g_tracks;
+  velo_track* tracks = pinned(c, g_tracks, g_tracks_cap, cap, "invokeParallelSearch");
   std::vector<uint32_t> counts(eventsToProcess), status(eventsToProcess);
   std::vector<uint64_t> first(eventsToProcess);
   velo_options opts;
@@ -165,22 +229,28 @@ void preorder_by_x(std::vector<const std::vector<uint8_t>*>& input) {
   if (bad.load() != 0) fail("preorder_by_x", (velo_status)bad.load(), nullptr);
 }
 
+// The reference sorts on the host (preorder_by_x), then searches in chunks of
+// 16000 events (GpuPixelSearchByTriplet.cpp:4-22,44-65); here each chunk is
+// sorted on the GPU as part of its search, with the same bytes left in the
+// caller's buffers and the same tracks.
 int independent_execute(const std::vector<std::vector<uint8_t> >& input,
                         std::vector<std::vector<uint8_t> >& output) {
   std::vector<const std::vector<uint8_t>*> converted(input.size());
   for (size_t i = 0; i < input.size(); ++i) converted[i] = &input[i];
   g_verbosity = 3;
   const auto t0 = std::chrono::steady_clock::now();
-  preorder_by_x(converted);
+  output.resize(input.size());
+  const int max_events_to_process_per_kernel = 16000;   // GpuPixelSearchByTriplet.cpp:53
+  for (size_t i = 0; i < input.size(); i += max_events_to_process_per_kernel) {
+    int n = (int)(input.size() - i);
+    if (n > max_events_to_process_per_kernel) n = max_events_to_process_per_kernel;
+    sort_and_search(converted, (int)i, n, output);
+  }
   const auto t1 = std::chrono::steady_clock::now();
-  const int r = gpuPixelSearchByTripletInvocation(converted, output);
-  const auto t2 = std::chrono::steady_clock::now();
-  const double sort_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
-  const double search_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
-  std::cout << "Sorted " << input.size() << " events on the host in " << sort_ms << " ms; searched them in "
-            << search_ms << " ms (" << (double)input.size() / ((sort_ms + search_ms) / 1e3)
-            << " events/s end to end)" << std::endl;
-  return r;
+  const double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  std::cout << "Sorted and searched " << input.size() << " events on the GPU in " << ms << " ms ("
+            << (double)input.size() / (ms / 1e3) << " events/s end to end)" << std::endl;
+  return 0;
 }
 
 void independent_post_execute(const std::vector<std::vector<uint8_t> >& output) {
