@@ -19,8 +19,10 @@
 
 #include <vector>
 
-/* Standalone entry: sorts each module's hits by x in place (through the
- * const input, as the reference does), then searches. */
+/* Standalone entry: sorts each module's hits by x, then searches.  The sort
+ * runs on the GPU, in chunks of at most 16000 events, with the reference's
+ * permutation; the sorted bytes are written back into the input (through the
+ * const reference, as the reference's host sort leaves them). */
 int independent_execute(const std::vector<std::vector<uint8_t> >& input,
                         std::vector<std::vector<uint8_t> >& output);
 
