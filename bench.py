@@ -2,8 +2,9 @@
 """Throughput of the GB300 search-by-triplet (events/s) on seeded synthetic VELO events.
 
 Default workload: 10,000 events from seeds 1000..10999 of the synthetic VELO
-generator (the plain path at scale, Y = 4, no FMA contraction), x-sorted by
-the reference sort before timing.
+generator (the plain path at scale, Y = 4, no FMA contraction), x-sorted
+before timing by the library's host sort (velo_sort_by_x: the reference's
+per-module permutation).
 
 The launch configuration is the autotuner's (velo_autotune: threads per
 event, shared-memory tile, register build, launch style; cached per workload
