@@ -27,9 +27,13 @@ the oracle restatement on all host cores, or with --ref-emulator the
 reference kernel itself under the work-group emulator (only where it was
 built from the reference sources).
 
-Multi-GPU (torchrun): weak scaling, every rank searches its own 10,000-event
-block (seeds offset by rank); no collective touches the data path, only a
-barrier and a max-reduction of the step time.
+Multi-GPU: weak scaling, every rank searches its own 10,000-event block
+(seeds offset by rank) on the GPU of its LOCAL_RANK; no collective touches
+the data path, only a barrier and max / sum reductions of the step time and
+event counts (gloo).  Under a launcher (torchrun) WORLD_SIZE must equal
+--gpus; without one, `--gpus N` (N > 1) starts the N ranks itself through
+torch.distributed.run on 127.0.0.1.  `--plan` prints the rank layout (world
+size and each rank's seed block) without touching a GPU.
 """
 from __future__ import annotations
 
@@ -84,6 +88,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-pruning leg")
     ap.add_argument("--no-stages", action="store_true", help="skip the device sort / fit leg")
+    ap.add_argument("--plan", action="store_true",
+                    help="print the rank layout (world size, seed block per rank) and exit; no GPU work")
     ap.add_argument("--ref-emulator", action="store_true",
                     help="reference arm: time the reference kernel under the work-group emulator "
                          "(oracle/_ref, only where it was built) instead of the oracle restatement")
@@ -132,6 +138,41 @@ def shard_seeds(first_seed: int, n_events: int, rank: int) -> range:
     """Weak scaling: rank r owns its own block of n_events seeds."""
     start = first_seed + rank * n_events
     return range(start, start + n_events)
+
+
+def launch_ranks(args):
+    """Ranks for --gpus N: under a launcher WORLD_SIZE must equal N (else exit
+    with an error); without one, N > 1 ranks are started here through
+    torch.distributed.run and their exit code is returned.  None: this
+    process is the (only) rank."""
+    world = os.environ.get("WORLD_SIZE")
+    if world is not None:
+        if int(world) != args.gpus:
+            sys.exit(f"bench.py: --gpus {args.gpus} but the launcher started WORLD_SIZE={world} ranks")
+        return None
+    if args.gpus <= 1:
+        return None
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
+def plan(args, ranks: "Ranks"):
+    """The rank layout this invocation would run, gathered on rank 0."""
+    first, n, _, _, _ = CONFIGS[args.config]
+    n = args.events or n
+    seeds = shard_seeds(first, n, ranks.rank)
+    mine = [ranks.rank, ranks.local, seeds.start, seeds.stop]
+    rows = [mine]
+    if ranks.pg:
+        rows = [None] * ranks.world
+        ranks.pg.all_gather_object(rows, mine)
+    return {"plan": True, "n_gpus": args.gpus, "world_size": ranks.world,
+            "ranks": [{"rank": r, "device": d, "seeds": [a, b]} for r, d, a, b in rows]}
 
 
 # -------------------------------------------------------------- workload --
@@ -567,9 +608,17 @@ def gpu_arm(args, ranks: Ranks):
 
 def main():
     args = parse_args()
+    rc = launch_ranks(args)
+    if rc is not None:
+        sys.exit(rc)
     ranks = Ranks()
     try:
-        line = reference_arm(args, ranks) if args.impl == "reference" else gpu_arm(args, ranks)
+        if args.plan:
+            line = plan(args, ranks)
+        elif args.impl == "reference":
+            line = reference_arm(args, ranks)
+        else:
+            line = gpu_arm(args, ranks)
         if line is not None and ranks.rank == 0:
             print(json.dumps(line), flush=True)
     finally:

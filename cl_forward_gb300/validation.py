@@ -169,6 +169,106 @@ def event_rates_fast(tracks: np.ndarray, hit_id: np.ndarray, truth: Truth, min_h
     return r
 
 
+_HASH_MUL = np.array([(0x9E3779B97F4A7C15 * (2 * k + 1)) & 0xFFFFFFFFFFFFFFFF for k in range(25)],
+                     np.uint64)
+
+
+def event_hashes(words: np.ndarray, counts: np.ndarray) -> np.ndarray:
+    """Order-independent digest of each event's tracks: the sum (mod 2**64) over
+    its tracks of a 64-bit hash of the whole 100-byte record.  Equal digests
+    mean equal track multisets (as hit-index lists in emitted order, zeros
+    past hitsNum) up to a 2**-64 collision.  ``words`` is (T, 25) uint32,
+    event by event; ``counts`` the tracks per event."""
+    counts = np.asarray(counts, np.int64)
+    out = np.zeros(len(counts), np.uint64)
+    if len(words) == 0:
+        return out
+    h = np.zeros(len(words), np.uint64)
+    with np.errstate(over="ignore"):
+        for k in range(25):
+            x = (words[:, k].astype(np.uint64) + np.uint64(k + 1)) * _HASH_MUL[k]
+            x ^= x >> np.uint64(29)
+            h = (h ^ x) * np.uint64(0xBF58476D1CE4E5B9)
+            h ^= h >> np.uint64(31)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    nz = counts > 0
+    with np.errstate(over="ignore"):
+        out[nz] = np.add.reduceat(h, starts[nz])
+    return out
+
+
+def hit_ids_packed(buf: np.ndarray, offsets: np.ndarray):
+    """Hit IDs of every event of a packed batch, concatenated, and each
+    event's first position in that array."""
+    parts = []
+    for o in offsets.tolist():
+        S, H = np.frombuffer(buf, "<i4", 2, o)
+        parts.append(np.frombuffer(buf, "<u4", int(H), o + 8 + 12 * int(S)))
+    ids = np.concatenate(parts) if parts else np.zeros(0, np.uint32)
+    lens = np.array([len(p) for p in parts], np.int64)
+    return ids, np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+
+
+def rates_packed(words: np.ndarray, counts: np.ndarray, hit_ids: np.ndarray, hit_base: np.ndarray,
+                 truths: Sequence[Truth], events: np.ndarray = None, min_hits: int = 3) -> Rates:
+    """:func:`rates` over a whole batch at once (same definitions).
+
+    ``words``/``counts`` as in :func:`event_hashes`; ``hit_ids``/``hit_base``
+    from :func:`hit_ids_packed`; ``events`` optionally restricts the rates to
+    a subset of event indices.  A track's majority key is the median of its
+    sorted hit keys: a key holding at least 70 % of the hits holds the middle
+    position, so the median is the only candidate the purity cut can accept.
+    """
+    n = len(counts)
+    counts = np.asarray(counts, np.int64)
+    sel = np.ones(n, bool) if events is None else np.isin(np.arange(n), events)
+    r = Rates()
+    nh_parts, p_parts, pbase = [], [], [0]
+    for t in truths:
+        nh_parts.append(np.asarray(t.n_hits))
+        p_parts.append(np.asarray(t.p))
+        pbase.append(pbase[-1] + len(t.n_hits))
+    nh = np.concatenate(nh_parts) if nh_parts else np.zeros(0, np.int64)
+    pp = np.concatenate(p_parts) if p_parts else np.zeros(0)
+    pbase = np.array(pbase, np.int64)
+    ev_of_particle = np.repeat(np.arange(n), np.diff(pbase))
+    recon = (nh >= min_hits) & sel[ev_of_particle]
+    low = pp < 2.0
+    r.reconstructible = int(recon.sum())
+    r.recon_low = int((recon & low).sum())
+    r.recon_high = int((recon & ~low).sum())
+    ev_of = np.repeat(np.arange(n), counts)
+    keep = sel[ev_of]
+    w = words[keep]
+    ev_of = ev_of[keep]
+    T = len(w)
+    r.tracks = T
+    if T == 0:
+        return r
+    nhit = w[:, 0].astype(np.int64)
+    mask = np.arange(24)[None, :] < nhit[:, None]
+    g = np.where(mask, w[:, 1:].astype(np.int64) + hit_base[ev_of][:, None], 0)
+    keys = np.where(mask, (hit_ids[g] >> np.uint32(8)).astype(np.int64), np.iinfo(np.int64).max)
+    keys.sort(axis=1)
+    med = keys[np.arange(T), nhit // 2]
+    cnt = (keys == med[:, None]).sum(axis=1)
+    matched = (med < NOISE_KEY_BASE) & (cnt >= PURITY * nhit)
+    r.ghosts = int((~matched).sum())
+    gk = ev_of[matched] * (1 << 32) + med[matched]
+    if len(gk):
+        uniq, mult = np.unique(gk, return_counts=True)
+        r.clones = int((mult - 1).sum())
+        e = uniq >> 32
+        k = (uniq & 0xFFFFFFFF) - 1
+        ok = (k >= 0) & (k < np.diff(pbase)[e])
+        pi = pbase[e[ok]] + k[ok]
+        good = recon[pi]
+        r.matched = int(good.sum())
+        r.matched_low = int((good & low[pi]).sum())
+        r.matched_high = int((good & ~low[pi]).sum())
+    return r
+
+
 def rates_fast(all_tracks, blobs: Sequence[bytes], truths: Sequence[Truth]) -> Rates:
     total = Rates()
     for t, b, tr in zip(all_tracks, blobs, truths):

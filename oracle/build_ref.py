@@ -18,7 +18,9 @@ work-group-shared under the emulator because all fibers of a work-group run
 on one OS thread.  Everything else is the reference's code, unmodified.
 
 Usage: ``python oracle/build_ref.py [--reference DIR]``; the reference
-checkout defaults to ``$CL_FORWARD_REFERENCE`` or ``/root/reference``.
+checkout is ``$CL_FORWARD_REFERENCE`` when set, else a checkout named
+``reference`` beside this repository; where neither exists, nothing is built
+and the tests that need the reference skip.
 """
 from __future__ import annotations
 
@@ -42,7 +44,10 @@ CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasi
 
 
 def default_reference() -> str:
-    return os.environ.get("CL_FORWARD_REFERENCE", "/root/reference")
+    env = os.environ.get("CL_FORWARD_REFERENCE")
+    if env:
+        return env
+    return os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 
 def available(reference: str | None = None) -> bool:

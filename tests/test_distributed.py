@@ -56,3 +56,36 @@ def test_reference_arm_runs_on_rank0_only(monkeypatch):
     args = A()
     r.rank = 1
     assert bench.reference_arm(args, r) is None
+
+
+def _bench(*argv, env_extra=None):
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    env.update(env_extra or {})
+    return subprocess.run([sys.executable, os.path.join(root, "bench.py"), *argv], capture_output=True, text=True,
+                          timeout=300, cwd=root, env=env)
+
+
+def test_gpus_flag_starts_that_many_ranks():
+    """`bench.py --gpus 2` without a launcher starts two ranks itself: the
+    printed n_gpus equals the world size, and the ranks own disjoint seed
+    blocks on devices 0 and 1."""
+    import json
+    r = _bench("--gpus", "2", "--plan", "--events", "30")
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == d["world_size"] == 2
+    ranks = sorted(d["ranks"], key=lambda x: x["rank"])
+    assert [x["device"] for x in ranks] == [0, 1]
+    assert ranks[0]["seeds"] == [1000, 1030] and ranks[1]["seeds"] == [1030, 1060]
+
+
+def test_gpus_flag_must_match_the_launcher():
+    r = _bench("--gpus", "2", "--plan", env_extra={"WORLD_SIZE": "3", "RANK": "0", "LOCAL_RANK": "0"})
+    assert r.returncode != 0 and "WORLD_SIZE=3" in r.stderr
+    r = _bench("--plan", "--events", "10")
+    assert r.returncode == 0 and '"world_size": 1' in r.stdout

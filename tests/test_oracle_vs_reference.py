@@ -10,7 +10,9 @@ import pytest
 
 from conftest import index_lists
 
-ref_dir = os.environ.get("CL_FORWARD_REFERENCE", "/root/reference")
+from oracle.build_ref import default_reference  # noqa: E402
+
+ref_dir = default_reference()
 
 
 @pytest.fixture(scope="module")

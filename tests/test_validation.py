@@ -64,3 +64,37 @@ def test_fast_rates_equal_reference_rates():
     slow = validation.rates(tracks, sb, truths)
     fast = validation.rates_fast(tracks, sb, truths)
     assert slow == fast
+
+
+def test_packed_helpers_equal_per_event_forms():
+    """The whole-batch forms used at 100,000 events (packed sort, chunked
+    restatement, digests, rates) equal the per-event ones."""
+    from oracle import oracle
+    blobs, truths = generator.generate(range(60), generator.CONFIG_BATCHED)
+    buf, offs, sizes = events.pack_events(blobs)
+    sbuf = oracle.sort_packed(buf, offs, sizes)
+    sb = [oracle.sort_by_x(b) for b in blobs]
+    assert [bytes(sbuf[int(o):int(o) + int(s)]) for o, s in zip(offs, sizes)] == sb
+    words, counts, status = oracle.search_packed(sbuf, offs, sizes, chunk=7)
+    tracks, st = oracle.search(sb, 4)
+    assert np.array_equal(status, st)
+    assert counts.tolist() == [len(t) for t in tracks]
+    assert np.array_equal(words, np.concatenate([t.view(np.uint32).reshape(-1, 25) for t in tracks]))
+    ids, base = validation.hit_ids_packed(sbuf, offs)
+    fast = validation.rates_packed(words, counts, ids, base, truths)
+    assert fast == validation.rates(tracks, sb, truths)
+    sub = np.arange(0, 60, 3)
+    assert validation.rates_packed(words, counts, ids, base, truths, events=sub) == \
+        validation.rates([tracks[e] for e in sub], [sb[e] for e in sub], [truths[e] for e in sub])
+    # digests: order-independent within an event, sensitive to any word
+    h = validation.event_hashes(words, counts)
+    perm = []
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    for e in range(60):
+        perm.extend((starts[e] + np.random.default_rng(e).permutation(counts[e])).tolist())
+    assert np.array_equal(validation.event_hashes(words[perm], counts), h)
+    w2 = words.copy()
+    w2[int(starts[5]), 3] ^= 1
+    h2 = validation.event_hashes(w2, counts)
+    assert h2[5] != h[5] and np.array_equal(np.delete(h2, 5), np.delete(h, 5))
+    assert len(set(h.tolist())) == 60
