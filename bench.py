@@ -22,6 +22,17 @@ Per step the GPU arm searches the whole batch once:
   cpu_baseline  the oracle restatement of the reference algorithm on all host
          cores over a bounded sample (rank 0 only).
   learned  the learned-pruned search of the same events (committed weights).
+  e2e_reference_api  the reference's own C++ entry points on
+         std::vector<std::vector<uint8_t>> input: independent_execute (unsorted
+         events; the x-sort and the search) and gpuPixelSearchByTriplet
+         (x-sorted events), host wall clock per call.
+  batched  100,000 uneven events (seeds 2000000..2099999): one persistent
+         launch, autotuned (on the first 20,000 events) and replayed from a
+         CUDA graph, beside the reference's launch style (one 256-thread CTA
+         per event), plus end to end in calls of 16,000 events.
+  stress  100,000 events at four times the pile-up (seeds 3000000..3099999):
+         plain against learned-pruned seeding, the fallback fraction, and
+         both methods' tracking rates on the first 10,000 events.
 `--impl reference` times the reference's algorithm on the host CPU instead:
 the oracle restatement on all host cores, or with --ref-emulator the
 reference kernel itself under the work-group emulator (only where it was
@@ -88,6 +99,14 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-pruning leg")
     ap.add_argument("--no-stages", action="store_true", help="skip the device sort / fit leg")
+    ap.add_argument("--no-reference-api", action="store_true",
+                    help="skip the end-to-end leg through the reference-signature C++ entry points")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched leg (100,000 uneven events, autotuned persistent launch + CUDA graph)")
+    ap.add_argument("--no-stress", action="store_true",
+                    help="skip the high-occupancy leg (100,000 events at 4x pile-up, plain vs learned)")
+    ap.add_argument("--batched-events", type=int, default=100000)
+    ap.add_argument("--stress-events", type=int, default=100000)
     ap.add_argument("--plan", action="store_true",
                     help="print the rank layout (world size, seed block per rank) and exit; no GPU work")
     ap.add_argument("--ref-emulator", action="store_true",
@@ -452,6 +471,238 @@ def learned_leg(ctx, hbuf, offs, sizes, blobs, truths, opts, tracks, counts, fir
             "note": "same events, same launch shape; the network is trained on other seeds (100000-149999)"}
 
 
+def pinned_pack(ctx, blobs):
+    """Events packed at 16-byte-aligned offsets in one pinned host buffer."""
+    import numpy as np
+    n = len(blobs)
+    offs = np.zeros(n, np.uint64)
+    sizes = np.array([len(b) for b in blobs], np.uint64)
+    total = 0
+    for i, b in enumerate(blobs):
+        offs[i] = total
+        total += (len(b) + 15) // 16 * 16
+    hbuf = ctx.host_alloc(max(total, 16))
+    for i, b in enumerate(blobs):
+        hbuf[int(offs[i]):int(offs[i]) + len(b)] = np.frombuffer(b, np.uint8)
+    return hbuf, offs, sizes
+
+
+class QuietStdout:
+    """Sends file descriptor 1 to /dev/null (the reference-signature entry
+    points print what the reference prints; stdout carries the JSON line)."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        self.null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self.null, 1)
+        return self
+
+    def __exit__(self, *a):
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        os.close(self.null)
+
+
+def reference_api_leg(raw, blobs, expected_tracks, args):
+    """End to end through the reference's own C++ entry points, on
+    std::vector<std::vector<uint8_t> > input and output (the timing harness
+    libvelo_api_bench.so): independent_execute on the unsorted events (sort
+    and search; GpuPixelSearchByTriplet.cpp:4-22) and gpuPixelSearchByTriplet
+    on the x-sorted ones (GpuPixelSearchByTriplet.cpp:29-37).  Host wall clock
+    per call; everything the call does is inside it."""
+    from cl_forward_gb300 import native
+    n = len(raw)
+    out = {"unit": "events/s", "events": n,
+           "io": "std::vector<std::vector<uint8_t>> per event in, output vectors allocated by each call"}
+    for entry, evs in (("independent_execute", raw), ("gpuPixelSearchByTriplet", blobs)):
+        with QuietStdout():
+            ms, tracks, _, _ = native.reference_api_times(evs, entry, max(args.warmup, 1), args.steps)
+        mean = statistics.fmean(ms)
+        out[entry] = {"value": n / (mean / 1e3), "ms_per_call": mean,
+                      "ms_samples": [round(float(x), 3) for x in ms], "tracks": tracks,
+                      "same_tracks_as_device_resident": tracks == expected_tracks}
+    return out
+
+
+def timed_steps(ctx, opts, args):
+    """Mean device milliseconds of args.steps runs (L2 flushed before each)."""
+    for _ in range(args.warmup):
+        ctx.run(opts)
+    ctx.synchronize()
+    steps_ms = [ctx.time_runs(opts, warmup=0, iters=1, flush_l2=True) for _ in range(args.steps)]
+    return statistics.fmean(steps_ms), steps_ms
+
+
+def tuned_on_sample(ctx, hbuf, offs, sizes, H, base, sample):
+    """Autotuned options for a large batch, tuned on its first `sample`
+    events (the sweep times 104 + 9 launch configurations)."""
+    from cl_forward_gb300 import autotune
+    k = min(sample, len(offs))
+    ctx.stage(hbuf, offs[:k], sizes[:k])
+    ctx.synchronize()
+    opts, info = autotune.tuned_options(ctx, k, float(H[:k].mean()), base, iters=3)
+    return opts, info
+
+
+def batched_leg(args, peak, peak_src):
+    """The batched configuration: 100,000 events of uneven size (PVs ~
+    Poisson(U(2, 30))), one persistent launch over all of them with the
+    autotuned configuration replayed from a CUDA graph, next to the launch
+    style of the reference's runs (one 256-thread CTA per event), and end to
+    end from pinned host buffers in calls of 16,000 events."""
+    import numpy as np
+    from cl_forward_gb300 import generator, native
+    first = CONFIGS["batched"][0]
+    raw, _ = generator.generate_parallel(range(first, first + args.batched_events), generator.CONFIG_BATCHED)
+    blobs = sort_events(raw)
+    del raw
+    S, H = workload_stats(blobs)
+    n = len(blobs)
+    ctx = native.Context(0)
+    hbuf, offs, sizes = pinned_pack(ctx, blobs)
+    del blobs
+    base = native.default_options(use_graph=1)
+    opts, tuned = tuned_on_sample(ctx, hbuf, offs, sizes, H, base, 20000)
+    opts.use_graph = 1
+    ctx.stage(hbuf, offs, sizes)
+    ms, samples = timed_steps(ctx, opts, args)
+    counts, _, status = ctx.fetch_counts(n)
+    T = counts.astype(np.int64)
+    alg = int((8 + 12 * S + 16 * H).sum() + (4 + 100 * T).sum())
+    style = native.default_options(launch_mode=0, threads_per_event=256, smem_hits=0, register_ctas=5,
+                                   seed_lanes=32, use_graph=1)
+    ms1, samples1 = timed_steps(ctx, style, args)
+    counts1, _, _ = ctx.fetch_counts(n)
+    # end to end through the C ABI, pinned host buffers, calls of 16,000 events
+    chunk = 16000
+    bounds = [(a, min(n, a + chunk)) for a in range(0, n, chunk)]
+    rows = np.maximum(H, 1).astype(np.int64)
+    out_cap = int(max(rows[a:b].sum() for a, b in bounds))
+    h_tracks = ctx.host_alloc(out_cap * 100).view(native.TRACK_DTYPE)
+    hc = np.zeros(n, np.uint32)
+    hf = np.zeros(n, np.uint64)
+    hs = np.zeros(n, np.uint32)
+    e2e_opts = native.Options.from_buffer_copy(opts)
+    e2e_opts.host_direct = 1
+    e2e_opts.use_graph = 0
+
+    def e2e_pass():
+        for a, b in bounds:
+            ctx.search_packed_into(hbuf, offs[a:b], sizes[a:b], e2e_opts, h_tracks, hc[a:b], hf[a:b], hs[a:b])
+
+    e2e_pass()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_pass()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    assert np.array_equal(hc, counts)
+    ctx.host_free(h_tracks.view(np.uint8))
+    ctx.host_free(hbuf)
+    ctx.close()
+    achieved = alg / (ms / 1e3) / 1e9
+    return {
+        "workload": CONFIGS["batched"][4], "events": n, "mean_hits": float(H.mean()), "max_hits": int(H.max()),
+        "min_hits": int(H.min()), "value": n / (ms / 1e3), "unit": "events/s", "ms_per_step": ms,
+        "ms_per_step_samples": [round(x, 3) for x in samples],
+        "launch": {"threads_per_event": opts.threads_per_event, "launch_mode": opts.launch_mode,
+                   "smem_hits": opts.smem_hits, "register_ctas": opts.register_ctas,
+                   "seed_lanes": opts.seed_lanes, "cuda_graph": True, "autotuned": tuned,
+                   "tuned_on": "the first 20,000 events of the batch"},
+        "config1_launch_style": {"value": n / (ms1 / 1e3), "ms_per_step": ms1,
+                                 "ms_per_step_samples": [round(x, 3) for x in samples1],
+                                 "launch": "one 256-thread CTA per event, automatic shared-memory tile, "
+                                           "32 seeding lanes per h0, CUDA graph",
+                                 "same_track_counts": bool(np.array_equal(counts1, counts))},
+        "speedup_vs_config1_launch_style": ms1 / ms,
+        "e2e": {"value": n / e2e_s, "unit": "events/s", "calls_of_events": chunk,
+                "io": "events read and tracks written in place in pinned host memory (NVLink-C2C)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "algorithmic_bytes": alg, "peak_source": peak_src,
+                     "achieved_config1_launch_style": alg / (ms1 / 1e3) / 1e9},
+        "tracks": int(T.sum()),
+        "status_flags": {"ring_overflow": int(np.sum(status & 1 != 0)),
+                         "track_overflow": int(np.sum(status & 2 != 0))},
+    }
+
+
+def stress_leg(args):
+    """The high-occupancy configuration: 100,000 events at four times the
+    pile-up, plain (autotuned, CUDA graph) against learned-pruned seeding on
+    the same launch, with the fraction of events that fall back to the plain
+    method; tracking rates of both, split at p = 2 GeV, on the first 10,000
+    events."""
+    import numpy as np
+    from cl_forward_gb300 import events as E, generator, native, validation
+    first = CONFIGS["stress"][0]
+    raw, truths = generator.generate_parallel(range(first, first + args.stress_events), generator.CONFIG_STRESS)
+    blobs = sort_events(raw)
+    del raw
+    S, H = workload_stats(blobs)
+    n = len(blobs)
+    ctx = native.Context(0)
+    hbuf, offs, sizes = pinned_pack(ctx, blobs)
+    base = native.default_options(use_graph=1)
+    opts, tuned = tuned_on_sample(ctx, hbuf, offs, sizes, H, base, 20000)
+    ctx.stage(hbuf, offs, sizes)
+    ms, samples = timed_steps(ctx, opts, args)
+    wz = np.load(LEARNED_WEIGHTS)
+    max_hits = int(wz["max_event_hits"]) if "max_event_hits" in wz.files else 0
+    ctx.set_mlp(wz["weights"], float(wz["keep_threshold"]), float(wz["window_margin"]),
+                float(wz["min_keep_rate"]), max_hits)
+    lo = native.Options.from_buffer_copy(opts)
+    lo.learned = 1
+    lo.use_graph = 0
+    ms_l, samples_l = timed_steps(ctx, lo, args)
+    _, _, lstatus = ctx.fetch_counts(n)
+    fallback = float(np.mean((lstatus & native.EVENT_LEARNED_FALLBACK) != 0))
+
+    # rates on the first 10,000 events, both methods
+    k = min(10000, n)
+    ctx.stage(hbuf, offs[:k], sizes[:k])
+    ids, base_ids = validation.hit_ids_packed(hbuf, offs[:k])
+    rates = {}
+    for name, o in (("plain", opts), ("learned", lo)):
+        o2 = native.Options.from_buffer_copy(o)
+        o2.use_graph = 0
+        ctx.run(o2)
+        counts, _, _ = ctx.fetch_counts(k)
+        cap = int(counts.sum())
+        tracks = np.zeros(max(cap, 1), E.TRACK_DTYPE)
+        c2 = np.zeros(k, np.uint32)
+        f2 = np.zeros(k, np.uint64)
+        s2 = np.zeros(k, np.uint32)
+        ctx.fetch_into(tracks, c2, f2, s2)
+        c64 = c2.astype(np.int64)
+        starts = np.concatenate([[0], np.cumsum(c64)[:-1]])
+        idx = np.repeat(f2.astype(np.int64) - starts, c64) + np.arange(cap, dtype=np.int64)
+        words = tracks.view(np.uint32).reshape(-1, 25)[:cap][idx]
+        rates[name] = validation.rates_packed(words, c64, ids, base_ids, truths[:k]).as_dict()
+    ctx.host_free(hbuf)
+    ctx.close()
+    rp, rl = rates["plain"], rates["learned"]
+    return {
+        "workload": CONFIGS["stress"][4], "events": n, "mean_hits": float(H.mean()), "max_hits": int(H.max()),
+        "plain": {"value": n / (ms / 1e3), "unit": "events/s", "ms_per_step": ms,
+                  "ms_per_step_samples": [round(x, 3) for x in samples],
+                  "launch": {"threads_per_event": opts.threads_per_event, "launch_mode": opts.launch_mode,
+                             "smem_hits": opts.smem_hits, "register_ctas": opts.register_ctas,
+                             "seed_lanes": opts.seed_lanes, "cuda_graph": True, "autotuned": tuned}},
+        "learned": {"value": n / (ms_l / 1e3), "unit": "events/s", "ms_per_step": ms_l,
+                    "ms_per_step_samples": [round(x, 3) for x in samples_l],
+                    "fallback_fraction": fallback, "max_event_hits": max_hits,
+                    "weights": os.path.relpath(LEARNED_WEIGHTS, ROOT)},
+        "learned_speedup_vs_plain": ms / ms_l,
+        "rates_first_10000_events": {"plain": rp, "learned": rl,
+                                     "efficiency_loss": rp["efficiency"] - rl["efficiency"],
+                                     "efficiency_loss_p_lt_2": rp["efficiency_p_lt_2"] - rl["efficiency_p_lt_2"],
+                                     "efficiency_loss_p_ge_2": rp["efficiency_p_ge_2"] - rl["efficiency_p_ge_2"],
+                                     "ghost_increase": rl["ghost_rate"] - rp["ghost_rate"],
+                                     "clone_change": rl["clone_rate"] - rp["clone_rate"]},
+    }
+
+
 # ---------------------------------------------------------------- GPU arm --
 def gpu_arm(args, ranks: Ranks):
     import numpy as np
@@ -600,9 +851,17 @@ def gpu_arm(args, ranks: Ranks):
         line["work"] = {"reference_evals_per_event": wk["window_evals"] + wk["forward_fits"] + wk["seed_fits"],
                         "reference_evals_per_s": (wk["window_evals"] + wk["forward_fits"] + wk["seed_fits"])
                         * value, "counted_by": "oracle restatement on 500 of the events"}
+    if ranks.rank == 0 and args.gpus == 1 and not args.no_reference_api:
+        line["e2e_reference_api"] = reference_api_leg(raw, blobs, int(T.sum()), args)
     ctx.host_free(hbuf)
     ctx.host_free(h_tracks.view(np.uint8))
     ctx.close()
+    if ranks.rank == 0 and args.gpus == 1 and args.config == "scale":
+        del raw, blobs
+        if not args.no_batched:
+            line["batched"] = batched_leg(args, peak, peak_src)
+        if not args.no_stress and os.path.exists(LEARNED_WEIGHTS):
+            line["stress"] = stress_leg(args)
     return line if ranks.rank == 0 else None
 
 

@@ -2,7 +2,8 @@
 
 The sweep itself is native (``velo_autotune`` in the C ABI): threads per
 event, hits staged per shared-memory tile, register build and launch style,
-timed on the caller's staged events.  This module caches the winner in a JSON
+then seeding lanes per h0 on the three fastest, timed on the caller's staged
+events.  This module caches the winner in a JSON
 file next to the built library, keyed by the device's SM count and the batch
 shape (event count and mean hits, bucketed to powers of two), so repeated
 runs of the same workload skip the sweep.
@@ -17,10 +18,10 @@ from typing import Optional, Tuple
 from . import native
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune_cache.json")
-FIELDS = ("threads_per_event", "launch_mode", "smem_hits", "narrow_windows", "register_ctas")
+FIELDS = ("threads_per_event", "launch_mode", "smem_hits", "narrow_windows", "register_ctas", "seed_lanes")
 
 
-SPACE = 6   # bumped when velo_autotune's candidate set changes: older entries are ignored
+SPACE = 7   # bumped when velo_autotune's candidate set changes: older entries are ignored
 
 
 def shape_key(sm_count: int, n_events: int, mean_hits: float, y_lanes: int) -> str:

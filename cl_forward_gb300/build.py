@@ -5,7 +5,9 @@ Outputs (in-tree, git-ignored), under ``cl_forward_gb300/_build/``:
 * ``libclforward_gb300.so`` -- the sm_103a kernels, the C ABI of
   ``include/velo_search.h`` and the reference-signature C++ entry points of
   ``include/GpuPixelSearchByTriplet.h`` (CUDA runtime linked statically);
-* ``clpixel`` -- the standalone driver (IndependentEntrypoint counterpart).
+* ``clpixel`` -- the standalone driver (IndependentEntrypoint counterpart);
+* ``libvelo_api_bench.so`` -- the timing harness of the reference-signature
+  entry points (bench.py's end-to-end leg through them).
 
 The kernels are compiled for ``sm_103a`` only, with ``--fmad=false`` so that no
 multiply-add contraction can change an FP32 cut (the kernel also spells every
@@ -31,6 +33,9 @@ BUILD = os.path.join(PKG, "_build")
 OBJ = os.path.join(BUILD, "obj")
 LIB = os.path.join(BUILD, "libclforward_gb300.so")
 DRIVER = os.path.join(BUILD, "clpixel")
+API_BENCH = os.path.join(BUILD, "libvelo_api_bench.so")
+# sources outside the library: the driver and the timing harness
+NOT_IN_LIB = ("clpixel_main.cpp", "velo_api_bench.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC",
@@ -86,7 +91,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *extra, *inc, "-c", src, "-o", obj])
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
         obj = os.path.join(OBJ, os.path.basename(src) + ".o")
-        if os.path.basename(src) != "clpixel_main.cpp":
+        if os.path.basename(src) not in NOT_IN_LIB:
             objs.append(obj)
         if force or _stale(obj, [src, *hdrs, __file__]):
             jobs.append(["g++", *CXX_FLAGS, *inc, "-c", src, "-o", obj])
@@ -107,6 +112,10 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     drv_obj = os.path.join(OBJ, "clpixel_main.cpp.o")
     if force or _stale(DRIVER, [LIB, drv_obj]):
         _run(["g++", "-o", DRIVER, drv_obj, "-L", BUILD, "-lclforward_gb300",
+              "-Wl,-rpath,$ORIGIN"], verbose)
+    bench_obj = os.path.join(OBJ, "velo_api_bench.cpp.o")
+    if force or _stale(API_BENCH, [LIB, bench_obj]):
+        _run(["g++", "-shared", "-o", API_BENCH, bench_obj, "-L", BUILD, "-lclforward_gb300",
               "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 

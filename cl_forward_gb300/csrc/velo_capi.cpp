@@ -263,6 +263,9 @@ void sort_range(float* a, float* b, float* c, uint32_t* d, int lo, int hi) {
   }
 }
 
+// Seeding lanes per h0 when the caller leaves the choice to the library.
+constexpr int32_t kDefaultSeedLanes = 16;
+
 uint32_t resolve_threads(int32_t t) {
   if (t == 32 || t == 64 || t == 128 || t == 256 || t == 512) return (uint32_t)t;
   return 256;
@@ -328,7 +331,10 @@ velo_status velo_sort_by_x(uint8_t* blob, uint64_t size) {
   float* z = y + H;
   int acc = 0;
   for (int m = 0; m < S; ++m) {
-    sort_range(x, y, z, id, acc, acc + num[m] - 1);
+    // strictly increasing x: the reference's partition moves nothing there
+    bool increasing = true;
+    for (int i = acc + 1; i < acc + num[m] && increasing; ++i) increasing = x[i - 1] < x[i];
+    if (!increasing) sort_range(x, y, z, id, acc, acc + num[m] - 1);
     acc += num[m];
   }
   return VELO_OK;
@@ -623,6 +629,15 @@ velo_status check_options(velo_ctx* c, const velo_options* opts, velo_options* o
     c->err = "pipeline_events must be >= 0";
     return VELO_ERR_INVALID_ARGUMENT;
   }
+  if (o->seed_lanes == 0) o->seed_lanes = kDefaultSeedLanes % o->y_lanes == 0 ? kDefaultSeedLanes : 32;
+  if (o->seed_lanes != 8 && o->seed_lanes != 16 && o->seed_lanes != 32) {
+    c->err = "seed_lanes must be 8, 16 or 32";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
+  if (o->seed_lanes < 32 && o->seed_lanes % o->y_lanes != 0) {
+    c->err = "seed_lanes below 32 must be a multiple of y_lanes";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
   if (o->register_ctas == 0) o->register_ctas = o->threads_per_event <= 64 ? 18 : 5;
   if (o->register_ctas != 4 && o->register_ctas != 5 && o->register_ctas != 18) {
     c->err = "register_ctas must be 4, 5 or 18";
@@ -691,6 +706,7 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
   p.order = P<int32_t>(c->d_order);
   p.n_events = c->n;
   p.y_lanes = o.y_lanes;
+  p.seed_lanes = o.seed_lanes;
   p.narrow = o.narrow_windows ? 1 : 0;
   p.persistent = o.launch_mode == VELO_LAUNCH_PERSISTENT ? 1 : 0;
   p.smem_arena_bytes = smem;
@@ -738,7 +754,8 @@ velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
   c->stats.smem_bytes_per_cta = (int32_t)smem;
   if (!o.use_graph) return enqueue_kernel(c, o, smem, grid);
   const uint64_t key[8] = {c->generation, smem, (uint64_t)grid, (uint64_t)o.threads_per_event,
-                           (uint64_t)o.register_ctas | ((uint64_t)o.learned << 8), (uint64_t)o.y_lanes,
+                           (uint64_t)o.register_ctas | ((uint64_t)o.learned << 8) | ((uint64_t)o.seed_lanes << 16),
+                           (uint64_t)o.y_lanes,
                            (uint64_t)o.narrow_windows, (uint64_t)o.launch_mode};
   if (!c->graph || std::memcmp(key, c->graph_key, sizeof key) != 0) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -1177,16 +1194,27 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
   velo_options b0;
   velo_status st = check_options(c, base, &b0);
   if (st != VELO_OK) return st;
-  // threads per event x shared-memory tile (hits staged per CTA; 0 = the
-  // automatic budget) x register build x launch style; narrowing stays on
-  // (it only removes work) and y_lanes is the caller's (it defines results)
-  // (32-thread CTAs are supported but measured far slower: 1.5x at best)
+  // median device milliseconds of `n` runs of `o`, L2 flushed before each
+  auto time_median = [&](const velo_options& o, int32_t n, float* med) -> velo_status {
+    std::vector<float> ms(n);
+    for (int32_t i = 0; i < n; ++i) {
+      velo_status s2 = velo_time_runs(c, &o, i == 0 ? 1 : 0, 1, 1, &ms[i]);
+      if (s2 != VELO_OK) return s2;
+    }
+    std::nth_element(ms.begin(), ms.begin() + n / 2, ms.end());
+    *med = ms[n / 2];
+    return VELO_OK;
+  };
+  // Stage 1: threads per event x shared-memory tile (hits staged per CTA;
+  // 0 = the automatic budget) x register build x launch style, at the
+  // caller's seed_lanes; narrowing stays on (it only removes work) and
+  // y_lanes is the caller's (it defines results).  32-thread CTAs are
+  // supported but measured far slower (1.5x at best).
   static const int32_t kThreads[] = {64, 128, 256, 512};
   static const int32_t kSmemHits[] = {0, 50, 100, 200, 300, 600, 900, 1200, 1600, 2400};
   static const int32_t kRegs[] = {4, 5, 18};
   static const int32_t kModes[] = {VELO_LAUNCH_PER_EVENT, VELO_LAUNCH_PERSISTENT};
-  float best = 0.f;
-  bool have = false;
+  std::vector<std::pair<float, velo_options>> stage1;
   for (int32_t mode : kModes)
     for (int32_t regs : kRegs)
       for (int32_t threads : kThreads)
@@ -1199,17 +1227,33 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
           o.threads_per_event = threads;
           o.smem_hits = hits;
           o.narrow_windows = 1;
-          std::vector<float> ms(iters);
-          for (int32_t i = 0; i < iters; ++i)
-            if ((st = velo_time_runs(c, &o, i == 0 ? 1 : 0, 1, 1, &ms[i])) != VELO_OK) return st;
-          std::nth_element(ms.begin(), ms.begin() + iters / 2, ms.end());
-          const float med = ms[iters / 2];
-          if (!have || med < best) {
-            best = med;
-            *best_out = o;
-            have = true;
-          }
+          float med = 0.f;
+          if ((st = time_median(o, iters, &med)) != VELO_OK) return st;
+          stage1.emplace_back(med, o);
         }
+  std::stable_sort(stage1.begin(), stage1.end(),
+                   [](const std::pair<float, velo_options>& a, const std::pair<float, velo_options>& b) {
+                     return a.first < b.first;
+                   });
+  // Stage 2: the three fastest launches x seeding lanes per h0 {8, 16, 32}
+  // (the seeding window's width; below 32 only multiples of y_lanes), each
+  // re-timed over more runs, so that near-equal launches are told apart.
+  const int32_t iters2 = std::max<int32_t>(4 * iters, 12);
+  float best = 0.f;
+  bool have = false;
+  for (size_t k = 0; k < stage1.size() && k < 3; ++k)
+    for (int32_t lanes : {8, 16, 32}) {
+      if (lanes < 32 && lanes % b0.y_lanes != 0) continue;
+      velo_options o = stage1[k].second;
+      o.seed_lanes = lanes;
+      float med = 0.f;
+      if ((st = time_median(o, iters2, &med)) != VELO_OK) return st;
+      if (!have || med < best) {
+        best = med;
+        *best_out = o;
+        have = true;
+      }
+    }
   if (best_ms_out) *best_ms_out = best;
   return VELO_OK;
 }

@@ -104,6 +104,7 @@ struct SearchParams {
   uint64_t out_capacity;          // rows of out_tracks; rows past it are not written
   int32_t n_events;
   int32_t y_lanes;
+  int32_t seed_lanes;             // lanes per h0 in seeding: 8, 16 or 32 (a multiple of y_lanes below 32)
   int32_t narrow;                 // 1 = binary-search narrowing of sorted modules
   int32_t persistent;
   uint32_t smem_arena_bytes;      // dynamic shared memory per CTA

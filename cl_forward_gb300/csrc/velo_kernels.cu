@@ -448,19 +448,46 @@ constexpr int kPlain = 0;    // the reference's seeding
 constexpr int kDump = 1;     // plain, recording sampled doublets as training data
 constexpr int kLearned = 2;  // MLP-pruned seeding
 
+// Lane constants of the seeding ballots.  A warp seeds 32 / G h0s at a time,
+// G lanes per h0 (a group); lane j of a group takes, in chunk c, h1 element
+// e = G c + j of its h0, which belongs to the reference's Y-lane e mod Y.
+struct SeedLanes {
+  int shift;              // log2(G)
+  uint32_t below_same;    // lanes of my group below me whose element shares my Y-lane
+  uint32_t same_all;      // every lane of my group whose element shares my Y-lane (Y | G)
+  uint32_t lane_mod;      // (lane mod G) mod Y: my Y-lane in chunk 0
+  uint32_t chunk_step;    // G mod Y: how far the Y-lanes turn per chunk (0 when Y | G)
+};
+
+__device__ __forceinline__ SeedLanes seed_lanes_of(int G, uint32_t Y) {
+  SeedLanes sl;
+  const int lane = threadIdx.x & 31;
+  sl.shift = G == 8 ? 3 : G == 16 ? 4 : 5;
+  const int jl = lane & (G - 1), gbase = lane - jl;
+  sl.below_same = 0;
+  for (int j = jl - (int)Y; j >= 0; j -= (int)Y) sl.below_same |= 1u << (gbase + j);
+  sl.same_all = 0;
+  for (int j = (int)((uint32_t)jl % Y); j < G; j += (int)Y) sl.same_all |= 1u << (gbase + j);
+  sl.lane_mod = (uint32_t)jl % Y;
+  sl.chunk_step = (uint32_t)G % Y;
+  return sl;
+}
+
 // Seeding of module f: h0 on f, h1 on f-2, h2 on f-4 (Kernel.cl:392-568
-// with the unused-h0 gather of :720-764).  One warp per h0; lane j of chunk c
-// takes h1 element e = 32c + j, which belongs to the reference's Y-lane
-// e mod Y.  New tracklets go to the back of ring[nb].
+// with the unused-h0 gather of :720-764).  Each group of G lanes takes one
+// h0 (SeedLanes); the warp walks the chunks of its groups' h1 windows
+// together, so the ballots and the groups' minimum reductions run with every
+// lane present.  New tracklets go to the back of ring[nb].
 template <int kMode, class Shared>
-__device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint32_t below_same_lane,
-                            uint32_t lane_mod) {
+__device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, const SeedLanes& sl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int G = 1 << sl.shift;
+  const int jl = lane & (G - 1);
+  const int groups = 32 >> sl.shift;
   const int st0 = s.start[f], n0 = s.num[f];
   const int s1 = f - 2, m4 = f - 4;
   const int st1 = s.start[s1], st4 = s.start[m4], n4 = s.num[m4];
   const uint32_t Y = (uint32_t)ev.Y;
-  const uint32_t chunk_step = 32u % Y;
   const float s1_z = s.num[s1] > 0 ? ev.zs()[st1] : 0.f;   // Kernel.cl:420
   const bool narrow4 = ev.narrow && s.sorted[m4] && n4 > 0;
   const float zmin4 = s.zmin[m4], zmax4 = s.zmax[m4];
@@ -473,24 +500,35 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
   uint32_t zk0 = 0x7fc00001u, zk1 = 0x7fc00001u;
   float dz_inv_cached = 0.f;
 
-  for (int i = warp; i < n0; i += nwarps) {
-    const int h0 = st0 + i;
-    if (ev.useds()[h0]) continue;                       // warp-uniform
-    const uint32_t w0 = ev.wins()[h0].x;
-    const uint32_t f1 = w0 & 0xffffu;
-    if (f1 == kNone16) continue;
-    const int n1 = (int)(w0 >> 16) - (int)f1;        // > 0 when a first hit was found
-    const float h0x = ev.xs()[h0], h0y = ev.ys()[h0], h0z = ev.zs()[h0];
+  for (int ib = warp * groups; ib < n0; ib += nwarps * groups) {   // warp-uniform
+    const int h0 = st0 + ib + (lane >> sl.shift);
+    int n1 = 0;
+    uint32_t f1 = 0;
+    if (h0 < st0 + n0 && !ev.useds()[h0]) {
+      const uint32_t w0 = ev.wins()[h0].x;
+      f1 = w0 & 0xffffu;
+      if (f1 != kNone16) n1 = (int)(w0 >> 16) - (int)f1;   // > 0 when a first hit was found
+    }
+    const int my_chunks = (n1 + G - 1) >> sl.shift;
+    const int chunks = G == 32 ? my_chunks : (int)__reduce_max_sync(kFull, (uint32_t)my_chunks);
+    if (chunks == 0) continue;                                      // warp-uniform
+    float h0x = 0.f, h0y = 0.f, h0z = 0.f;
+    if (n1 > 0) {
+      h0x = ev.xs()[h0];
+      h0y = ev.ys()[h0];
+      h0z = ev.zs()[h0];
+    }
     const float dymax = fmul(kMaxYSlope, fabsf(fsub(s1_z, h0z)));
     H0Features g0{};
     if constexpr (kMode != kPlain) g0 = h0_features(h0x, h0y, f, ev.S, dymax);
     unsigned long long best = ~0ull;
-    uint32_t dead_lanes = 0;                         // Y-lanes already stopped (bit per lane)
+    bool lane_dead = false;                          // Y | G: my Y-lane has stopped
+    uint32_t dead_lanes = 0;                         // otherwise (G = 32): Y-lanes stopped, bit per lane
     uint32_t chunk_mod = 0;
-    for (int c = 0; c < n1; c += 32) {
-      const int e = c + lane;
+    for (int c = 0; c < chunks << sl.shift; c += G) {
+      const int e = c + jl;
       const bool in = e < n1;
-      uint32_t ly = lane_mod + chunk_mod;
+      uint32_t ly = sl.lane_mod + chunk_mod;
       if (ly >= Y) ly -= Y;
       const int h1 = st1 + (int)f1 + e;
       // everything the cuts read about h1, loaded at once (one round trip)
@@ -506,10 +544,16 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
       }
       const bool dead = in && (w1 & 0xffffu) == kNone16;
       const unsigned dmask = __ballot_sync(kFull, dead);
-      const bool stopped = ((dmask & below_same_lane) != 0) || ((dead_lanes >> ly) & 1u);
-      dead_lanes |= __reduce_or_sync(kFull, dead ? (1u << ly) : 0u);
-      chunk_mod += chunk_step;
-      if (chunk_mod >= Y) chunk_mod -= Y;
+      bool stopped;
+      if (sl.chunk_step == 0) {   // a lane's Y-lane is the same in every chunk
+        stopped = (dmask & sl.below_same) != 0 || lane_dead;
+        lane_dead = lane_dead || (dmask & sl.same_all) != 0;
+      } else {                    // G = 32, Y does not divide 32: the Y-lanes turn per chunk
+        stopped = ((dmask & sl.below_same) != 0) || ((dead_lanes >> ly) & 1u);
+        dead_lanes |= __reduce_or_sync(kFull, dead ? (1u << ly) : 0u);
+        chunk_mod += sl.chunk_step;
+        if (chunk_mod >= Y) chunk_mod -= Y;
+      }
       bool cand = in && !dead && !stopped && !u1;
       if (cand) cand = fabsf(fsub(h1y, h0y)) < dymax;   // h2-independent term of Kernel.cl:509
       int a = (int)(w1 & 0xffffu), b = (int)(w1 >> 16);
@@ -606,22 +650,32 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, uint3
         best = key < best ? key : best;
       }
     }
-    {   // 64-bit minimum as two 32-bit warp reductions: the high words, then
-        // the low words of the lanes that hold the minimal high word
-      const uint32_t hi = (uint32_t)(best >> 32);
-      const uint32_t hmin = __reduce_min_sync(kFull, hi);
-      const uint32_t lmin = __reduce_min_sync(kFull, hi == hmin ? (uint32_t)best : 0xffffffffu);
-      best = ((unsigned long long)hmin << 32) | lmin;
+    // the group's 64-bit minimum as two 32-bit minima: the high words, then
+    // the low words of the lanes that hold the minimal high word
+    const uint32_t hi = (uint32_t)(best >> 32);
+    uint32_t hmin, lmin;
+    if (G == 32) {
+      hmin = __reduce_min_sync(kFull, hi);
+      lmin = __reduce_min_sync(kFull, hi == hmin ? (uint32_t)best : 0xffffffffu);
+    } else {   // butterflies inside each group of G lanes
+      hmin = hi;
+      for (int o = G >> 1; o > 0; o >>= 1) hmin = min(hmin, __shfl_xor_sync(kFull, hmin, o));
+      lmin = hi == hmin ? (uint32_t)best : 0xffffffffu;
+      for (int o = G >> 1; o > 0; o >>= 1) lmin = min(lmin, __shfl_xor_sync(kFull, lmin, o));
     }
-    if (lane == 0 && best != ~0ull) {   // Kernel.cl:550-567
+    best = ((unsigned long long)hmin << 32) | lmin;
+    // Kernel.cl:550-567: each group's first lane appends the group's tracklet
+    // (one shared-memory atomic per warp for the tracklet rows, one for the ring)
+    const bool win = jl == 0 && best != ~0ull;
+    const uint32_t tp = warp_reserve(&s.ntracklets, win);
+    const bool push = win && tp < ev.cap;
+    const uint32_t ri = warp_reserve(&s.ring_hi[nb], push);
+    if (push) {
       const uint32_t e = (uint32_t)(best >> 14) & 0x3fffu;
       const uint32_t h1 = (uint32_t)(st1 + (int)f1) + e;
       const uint32_t h2 = (uint32_t)st4 + (uint32_t)(best & 0x3fffu);
-      const uint32_t tp = atomicAdd(&s.ntracklets, 1u);
-      if (tp < ev.cap) {
-        ev.tracklets[tp] = make_uint4((uint32_t)h0, h1, h2, 0u);
-        push_back(s, ev, nb, make_uint4(kTrackletFlag | tp, (uint32_t)h0, h1, h2));
-      }
+      ev.tracklets[tp] = make_uint4((uint32_t)h0, h1, h2, 0u);
+      if (ri < ev.ring_cap) ring_buf(ev, nb)[ev.ring_cap - 1u - ri] = make_uint4(kTrackletFlag | tp, (uint32_t)h0, h1, h2);
     }
   }
   if (degenerate) atomicOr(&s.status, VELO_EVENT_DEGENERATE);
@@ -776,12 +830,9 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     compute_windows(ev, s, h, lo);
   }
 
-  // per-lane constants of the seeding ballots: lanes j < lane in the same
-  // Y-lane (j = lane mod Y), and lane mod Y
-  const uint32_t Y = (uint32_t)ev.Y;
-  uint32_t below_same_lane = 0;
-  for (int j = lane - (int)Y; j >= 0; j -= (int)Y) below_same_lane |= 1u << j;
-  const uint32_t lane_mod = (uint32_t)lane % Y;
+  // per-lane constants of the seeding ballots (the host checked that
+  // seed_lanes is 8, 16 or 32, and a multiple of Y below 32)
+  const SeedLanes sl = seed_lanes_of(p.seed_lanes, (uint32_t)ev.Y);
   __syncthreads();
   VELO_PHASE(2);
 
@@ -816,9 +867,9 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       }
       if (s.num[f] > 0) {
         if (learned)
-          seed_module<kLearned>(ev, s, f, b ^ 1, below_same_lane, lane_mod);
+          seed_module<kLearned>(ev, s, f, b ^ 1, sl);
         else
-          seed_module<kMode == kDump ? kDump : kPlain>(ev, s, f, b ^ 1, below_same_lane, lane_mod);
+          seed_module<kMode == kDump ? kDump : kPlain>(ev, s, f, b ^ 1, sl);
       }
       __syncthreads();
       VELO_PHASE(4);

@@ -143,7 +143,12 @@ __global__ void __launch_bounds__(kPrepThreads) static_prep_kernel(const uint8_t
 }
 
 std::mutex g_mutex;
-void* g_scratch_ptr[64] = {};   // device address of the array, per device ordinal
+// Device address of the array, per device ordinal, taken on the first call
+// with that device current and kept for the life of the process: it belongs
+// to the device's primary context (the one the CUDA runtime uses), so it
+// goes stale if that context is destroyed (cudaDeviceReset) and a new one
+// made; the entry point's header says so.
+void* g_scratch_ptr[64] = {};
 uint32_t g_configured_smem[64] = {};
 
 }  // namespace
@@ -157,7 +162,8 @@ extern "C" velo_status velo_search_device_static(const uint8_t* d_input, const u
   using namespace velo;
   if (n_events < 0 || n_events > VELO_STATIC_MAX_EVENTS) return VELO_ERR_CAPACITY;
   if (total_hits + (uint64_t)n_events > VELO_STATIC_MAX_HIT_ROWS) return VELO_ERR_CAPACITY;
-  if (max_event_hits > VELO_STATIC_MAX_HIT_ROWS || y_lanes < 1 || y_lanes > 16) return VELO_ERR_INVALID_ARGUMENT;
+  if (max_event_hits > VELO_STATIC_MAX_HIT_ROWS) return VELO_ERR_CAPACITY;   // no such event can be staged
+  if (y_lanes < 1 || y_lanes > 16) return VELO_ERR_INVALID_ARGUMENT;
   if (track_capacity < total_hits + (uint64_t)n_events) return VELO_ERR_CAPACITY;
   if (n_events > 0 && (!d_input || !d_offsets || !d_sizes || !d_tracks_out || !d_counts || !d_first || !d_status))
     return VELO_ERR_INVALID_ARGUMENT;
@@ -201,6 +207,7 @@ extern "C" velo_status velo_search_device_static(const uint8_t* d_input, const u
   p.order = nullptr;
   p.n_events = n_events;
   p.y_lanes = y_lanes;
+  p.seed_lanes = 32;
   p.narrow = 1;
   p.persistent = 0;
   p.smem_arena_bytes = smem;

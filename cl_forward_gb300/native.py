@@ -68,7 +68,7 @@ class Options(ctypes.Structure):
                 ("use_graph", ctypes.c_int32), ("register_ctas", ctypes.c_int32),
                 ("learned", ctypes.c_int32), ("pipeline_events", ctypes.c_int32),
                 ("host_direct", ctypes.c_int32), ("device_budget_mb", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("seed_lanes", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class Stats(ctypes.Structure):
@@ -347,6 +347,48 @@ class Context:
 
     def host_free(self, arr: np.ndarray):
         self._check(self._lib.velo_host_free(self._h, ctypes.c_void_p(arr.ctypes.data)), "velo_host_free")
+
+
+API_BENCH_PATH = os.path.join(PKG, "_build", "libvelo_api_bench.so")
+
+
+def reference_api_times(blobs: Sequence[bytes], entry: str, warmup: int, steps: int, want_sorted: bool = False):
+    """Host wall-clock milliseconds of `steps` calls of a reference-signature
+    entry point on std::vector<std::vector<uint8_t> > input (the timing
+    harness libvelo_api_bench.so): entry "independent_execute" (unsorted
+    events; sort and search) or "gpuPixelSearchByTriplet" (x-sorted events).
+    Returns (ms per call, tracks of the last call, each event's output
+    digest as validation.event_hashes computes it, the input bytes after the
+    last call or None).  The entry points
+    print what the reference prints; that text goes to this process's
+    stdout, so callers that own stdout redirect it around the call."""
+    load()
+    if not os.path.exists(API_BENCH_PATH):
+        raise RuntimeError(f"timing harness missing: {API_BENCH_PATH}; run cl_forward_gb300.build.build()")
+    lib = ctypes.CDLL(API_BENCH_PATH)
+    vp = ctypes.c_void_p
+    lib.velo_bench_reference_api.argtypes = [vp, vp, vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.c_int32, vp, vp, vp, vp]
+    n = len(blobs)
+    sizes = np.array([len(b) for b in blobs], np.uint64)
+    offs = np.zeros(n, np.uint64)
+    if n:
+        offs[1:] = np.cumsum(sizes)[:-1]
+    buf = np.frombuffer(b"".join(blobs), np.uint8) if n else np.zeros(1, np.uint8)
+    ms = np.zeros(max(steps, 1), np.float64)
+    tracks = ctypes.c_uint64()
+    digests = np.zeros(max(n, 1), np.uint64)
+    out = np.zeros(max(int(sizes.sum()), 1), np.uint8) if want_sorted else None
+    code = {"independent_execute": 0, "gpuPixelSearchByTriplet": 1}[entry]
+    st = lib.velo_bench_reference_api(buf.ctypes.data, _p(offs), _p(sizes), n, code, warmup, steps, _p(ms),
+                                      ctypes.byref(tracks), _p(digests),
+                                      _p(out) if out is not None else None)
+    if st != 0:
+        raise RuntimeError("velo_bench_reference_api: bad arguments")
+    sorted_blobs = None
+    if out is not None:
+        sorted_blobs = [out[int(o):int(o) + int(z)].tobytes() for o, z in zip(offs, sizes)]
+    return ms[:steps].copy(), int(tracks.value), digests[:n].copy(), sorted_blobs
 
 
 def _check_free(st: int, what: str):

@@ -106,7 +106,13 @@ typedef struct velo_options {
   int32_t device_budget_mb;   /* velo_search / velo_search_packed: device memory one call may
                                  use; a batch that needs more (about 275 B per hit) is cut into
                                  pipelined parts that fit.  0 = half the free device memory */
-  int32_t reserved[4];
+  int32_t seed_lanes;         /* seeding: lanes given to one h0's h1 candidates, 8, 16 or 32 (a
+                                 warp then seeds 32 / seed_lanes h0s at once); below 32 it must
+                                 be a multiple of y_lanes.  The width of the seeding window a
+                                 warp slides over an h0's h1 candidates (the reference's Y-lanes
+                                 per h0, Kernel.cl:435-436, set how many work-items share one
+                                 h0).  Results do not depend on it.  0 = automatic */
+  int32_t reserved[3];
 } velo_options;
 
 typedef struct velo_stats {
@@ -199,11 +205,15 @@ velo_status velo_get_stats(const velo_ctx* ctx, velo_stats* stats);
 velo_status velo_time_runs(velo_ctx* ctx, const velo_options* opts, int32_t warmup, int32_t iters,
                            int32_t flush_l2, float* ms_out);
 
-/* Autotuner: times the staged events under a grid of launch configurations
- * (threads per event {128, 256} x shared-memory tile {auto, 600, 900, 1200,
- * 1600, 2400 hits} x register build {4, 5} x launch style {per event,
- * persistent}), `iters` timed runs each with L2 flushed, and returns the
- * fastest (median) in best_out, its milliseconds in best_ms_out.  Every
+/* Autotuner, in two stages on the staged events, every run with L2 flushed.
+ * Stage 1 times a grid of launch configurations, `iters` runs each: threads
+ * per event {64, 128, 256, 512} x shared-memory tile {auto, 50, 100, 200,
+ * 300, 600, 900, 1200, 1600, 2400 hits} x register build {4, 5, 18} x launch
+ * style {per event, persistent}, where the 18-CTA build is the 64-thread one
+ * and only build 5 runs 512 threads (104 configurations).  Stage 2 takes the
+ * three fastest and times each with seed_lanes 8, 16 and 32 (below 32 only
+ * multiples of y_lanes) over max(4 iters, 12) runs.  best_out gets the
+ * fastest median of stage 2, best_ms_out its milliseconds.  Every
  * configuration gives the same tracks; y_lanes and use_graph are taken from
  * `base`. */
 velo_status velo_autotune(velo_ctx* ctx, const velo_options* base, int32_t iters,
@@ -283,9 +293,12 @@ int32_t velo_device_sm_count(const velo_ctx* ctx);
  * their declared bounds get VELO_EVENT_INVALID and no tracks.
  *
  * The first call on a device takes the array's device address (with that
- * device current), so make that first call before any stream capture.  Every
- * call reuses the same array: calls whose GPU work overlaps (other streams,
- * other host threads) race and must be serialised by the caller.
+ * device current), so make that first call before any stream capture.  The
+ * address is kept for the life of the process and belongs to the device's
+ * primary context, the one the CUDA runtime uses: call this entry point with
+ * that context current, and not again after cudaDeviceReset on the device.
+ * Every call reuses the same array: calls whose GPU work overlaps (other
+ * streams, other host threads) race and must be serialised by the caller.
  */
 #define VELO_STATIC_MAX_EVENTS 4096
 #define VELO_STATIC_MAX_HIT_ROWS 131072

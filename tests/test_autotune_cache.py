@@ -10,6 +10,7 @@ class FakeOptions:
         self.smem_hits = 0
         self.narrow_windows = 1
         self.register_ctas = 5
+        self.seed_lanes = 32
         self.__dict__.update(kw)
 
 
@@ -21,7 +22,7 @@ class FakeCtx:
 
     def autotune(self, base, iters):
         self.calls += 1
-        return FakeOptions(threads_per_event=128, launch_mode=1, smem_hits=900, register_ctas=4), 5.5
+        return FakeOptions(threads_per_event=128, launch_mode=1, smem_hits=900, register_ctas=4, seed_lanes=8), 5.5
 
 
 def test_shape_key_buckets():
@@ -38,6 +39,6 @@ def test_tune_once_then_cached(tmp_path, monkeypatch):
     o2, info2 = autotune.tuned_options(ctx, 10000, 1161, iters=2, cache_path=path)
     assert ctx.calls == 1 and not info1["cached"] and info2["cached"]
     for o in (o1, o2):
-        assert (o.threads_per_event, o.launch_mode, o.smem_hits, o.register_ctas) == (128, 1, 900, 4)
+        assert (o.threads_per_event, o.launch_mode, o.smem_hits, o.register_ctas, o.seed_lanes) == (128, 1, 900, 4, 8)
     autotune.tuned_options(ctx, 10000, 1161, iters=2, cache_path=path, refresh=True)
     assert ctx.calls == 2

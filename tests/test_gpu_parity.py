@@ -36,11 +36,13 @@ def _assert_same(gpu_ctx, oracle_lib, blobs, y=4, **opts):
     return got, checked
 
 
+@pytest.mark.parametrize("lanes", [8, 16, 32])
 @pytest.mark.parametrize("name", GOLDEN_SETS)
 @pytest.mark.parametrize("y", GOLDEN_Y)
-def test_golden_vectors(gpu_ctx, golden, name, y):
+def test_golden_vectors(gpu_ctx, golden, name, y, lanes):
+    """The reference kernel's own outputs, with every seeding width (lanes per h0)."""
     from cl_forward_gb300 import native
-    got, status = gpu_ctx.search(golden[name]["sorted"], native.default_options(y_lanes=y))
+    got, status = gpu_ctx.search(golden[name]["sorted"], native.default_options(y_lanes=y, seed_lanes=lanes))
     assert not np.any(status)
     for e, ref in enumerate(golden[name]["tracks"][y]):
         assert index_lists(got[e]) == index_lists_words(ref), f"{name} event {e}"
@@ -56,15 +58,34 @@ def test_config_small_100_events(gpu_ctx, oracle_lib):
     assert n == 100
 
 
-@pytest.mark.parametrize("y", [1, 2, 3, 4, 16])
-def test_fuzz_ties_and_lanes(gpu_ctx, oracle_lib, y):
+@pytest.mark.parametrize("y,lanes", [(1, 8), (1, 32), (2, 16), (3, 32), (4, 8), (4, 16), (4, 32), (8, 8),
+                                     (16, 16), (16, 32)])
+def test_fuzz_ties_and_lanes(gpu_ctx, oracle_lib, y, lanes):
+    """Exact fit ties and wide h1 windows: the winner's (fit, Y-lane, h1, h2)
+    order and each Y-lane's stop at its first h1 without an h2 window must
+    hold whether one h0's candidates span one warp or a group of 8 or 16
+    lanes (several chunks per group, Y-lanes that do or do not divide 32)."""
     from cl_forward_gb300 import fuzz
     blobs = [fuzz.fuzz_event(5000 + s, max_per_module=20, grid=1.0, lines=10, x_span=45) for s in range(150)]
     blobs += [fuzz.fuzz_event(2000 + s, jitter_z=True) for s in range(50)]
     blobs += [fuzz.fuzz_event(s, grid=2.0) for s in range(50)]
     blobs += [fuzz.fuzz_event(3000 + s, n_modules=3 + s % 20) for s in range(40)]
-    _, n = _assert_same(gpu_ctx, oracle_lib, _sorted(oracle_lib, blobs), y=y)
+    blobs += [fuzz.fuzz_event(7000 + s, max_per_module=60, grid=0.5, lines=30, x_span=20) for s in range(40)]
+    _, n = _assert_same(gpu_ctx, oracle_lib, _sorted(oracle_lib, blobs), y=y, seed_lanes=lanes)
     assert n > 200
+
+
+@pytest.mark.parametrize("y,lanes", [(4, 12), (4, 64), (3, 8), (3, 16), (8, 4), (16, 8)])
+def test_seed_lanes_rejected(gpu_ctx, oracle_lib, y, lanes):
+    """Seeding widths other than 8, 16 and 32, or below 32 and not a multiple of Y."""
+    from cl_forward_gb300 import generator, native
+    blobs = _sorted(oracle_lib, generator.generate(range(2))[0])
+    with pytest.raises(native.VeloError) as err:
+        gpu_ctx.search(blobs, native.default_options(y_lanes=y, seed_lanes=lanes))
+    assert err.value.status == native.ERR_INVALID_ARGUMENT
+    got, _ = gpu_ctx.search(blobs, native.default_options(y_lanes=y))   # automatic width
+    want, _ = oracle_lib.search(blobs, y)
+    assert [index_lists(g) for g in got] == [index_lists(w) for w in want]
 
 
 @pytest.mark.parametrize("threads", [32, 64, 128, 256, 512])
@@ -249,6 +270,29 @@ def test_device_sort_matches_reference_sort(gpu_ctx, oracle_lib, golden):
     for e in range(len(raw)):
         if not (status[e] & OVERFLOW_BITS):
             assert index_lists(got[e]) == index_lists(want[e])
+
+
+def test_device_sort_of_sorted_crowded_modules(gpu_ctx, oracle_lib):
+    """Sorting events whose modules are already x-sorted changes nothing and
+    takes one pass per module: with 16,383-hit modules the reference's
+    first-element pivots would walk ~1.3e8 steps in one thread each."""
+    import time
+    from cl_forward_gb300 import events, fuzz, generator
+    raw = [fuzz.crowded_event(s, 16383, module=m) for s, m in ((1, 38), (2, 39), (3, 20))]
+    raw += generator.generate(range(2100, 2110))[0]
+    want = [oracle_lib.sort_by_x(b) for b in raw]
+    for batch, expect in ((raw, want), (want, want)):
+        buf, offs, sizes = events.pack_events(batch)
+        gpu_ctx.stage(buf, offs, sizes)
+        gpu_ctx.synchronize()
+        t0 = time.perf_counter()
+        gpu_ctx.sort_staged()
+        gpu_ctx.synchronize()
+        dt = time.perf_counter() - t0
+        staged = gpu_ctx.fetch_staged(len(buf))
+        got = [bytes(staged[int(o):int(o) + int(n)]) for o, n in zip(offs, sizes)]
+        assert got == expect
+    assert dt < 0.1, f"re-sorting sorted events took {dt * 1e3:.1f} ms"
 
 
 def test_track_fits_match_least_squares(gpu_ctx, oracle_lib):

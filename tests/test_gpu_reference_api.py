@@ -69,8 +69,8 @@ def test_cpp_driver_dump(native_lib, oracle_lib, tmp_path):
 
 
 def test_cpp_driver_sorts_many_events_in_parallel(native_lib, oracle_lib, tmp_path):
-    """independent_execute through the C++ driver on 150 events: the host
-    sort then runs on several threads; every event keeps the reference's
+    """independent_execute through the C++ driver on 150 events: the events
+    are sorted on the GPU (velo_sort_staged) with the reference's
     permutation, so the dumped tracks match the oracle's on the sorted events."""
     from cl_forward_gb300 import build, events, generator
     raw = generator.generate(range(300, 450))[0]
@@ -93,3 +93,28 @@ def test_cpp_driver_sorts_many_events_in_parallel(native_lib, oracle_lib, tmp_pa
                      for _, _, body in tracks)
         ev = events.unpack_event(oracle_lib.sort_by_x(raw[e]))
         assert ids == sorted(tuple(sorted(int(ev.hit_id[h]) for h in t)) for t in index_lists(want[e]))
+
+
+def test_reference_entry_points_on_vectors(native_lib, oracle_lib):
+    """The reference-signature entry points on std::vector input, through the
+    timing harness: independent_execute leaves the caller's buffers sorted
+    byte for byte as the reference's preorder_by_x does (Tools.cpp:46-66);
+    its output vectors and gpuPixelSearchByTriplet's on the sorted events
+    hold the oracle's tracks, event by event.  20,000 events: two chunks of
+    at most 16,000 (GpuPixelSearchByTriplet.cpp:53)."""
+    from cl_forward_gb300 import generator, native, validation
+    raw = generator.generate_parallel(range(20000, 40000))[0]
+    ms, tracks_ie, dig_ie, after = native.reference_api_times(raw, "independent_execute", 0, 1, want_sorted=True)
+    want_sorted = [oracle_lib.sort_by_x(b) for b in raw]
+    assert after == want_sorted
+    ms2, tracks_gp, dig_gp, untouched = native.reference_api_times(want_sorted, "gpuPixelSearchByTriplet", 0, 1,
+                                                                   want_sorted=True)
+    assert untouched == want_sorted                    # the framework entry does not sort
+    assert tracks_ie == tracks_gp and np.array_equal(dig_ie, dig_gp)
+    want, wst = oracle_lib.search(want_sorted, 4)
+    words = np.concatenate([w.view(np.uint32).reshape(-1, 25) for w in want])
+    ohash = validation.event_hashes(words, np.array([len(w) for w in want]))
+    compared = np.flatnonzero((wst & oracle_lib.PARITY_EXCLUDING) == 0)
+    assert len(compared) > 19900
+    assert np.array_equal(dig_gp[compared], ohash[compared])
+    assert ms[0] > 0 and ms2[0] > 0

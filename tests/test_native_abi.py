@@ -46,6 +46,27 @@ def test_reference_cpp_entry_points_are_exported(native_lib):
         assert sym in out, sym
 
 
+def test_reference_api_timing_harness_builds(native_lib):
+    """bench.py's harness for the reference-signature entry points loads (it
+    links the library) and exports its one timing call."""
+    import ctypes
+    from cl_forward_gb300 import native
+    assert os.path.exists(native.API_BENCH_PATH)
+    assert "velo_bench_reference_api" in _exported(native.API_BENCH_PATH)
+    lib = ctypes.CDLL(native.API_BENCH_PATH)
+    lib.velo_bench_reference_api.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 4
+    assert lib.velo_bench_reference_api(None, None, None, -1, 0, 0, 1, None, None, None, None) == -1
+    assert lib.velo_bench_reference_api(None, None, None, 0, 2, 0, 1, None, None, None, None) == -1
+
+
+def test_seed_lanes_field_keeps_the_options_layout():
+    """seed_lanes took one of the reserved words: the structure is 64 bytes."""
+    import ctypes
+    from cl_forward_gb300 import native
+    assert ctypes.sizeof(native.Options) == 64
+    assert native.Options.seed_lanes.offset == 48
+
+
 def test_no_forbidden_cuda_calls_in_sources():
     bad = re.compile(r"cu(da)?Memcpy(3D)?BatchAsync")
     for d in ("cl_forward_gb300/csrc", "include"):

@@ -111,8 +111,8 @@ def test_static_limits_are_rejected(lib_and_ctx):
     total = sum(_hits(b) for b in batch)
     assert _call_static(lib, batch, total_hits=native.STATIC_MAX_HIT_ROWS)[0] == native.ERR_CAPACITY
     assert _call_static(lib, batch, capacity=total)[0] == native.ERR_CAPACITY
-    assert _call_static(lib, batch, max_event_hits=100000)[0] in (native.ERR_CAPACITY,
-                                                                   native.ERR_INVALID_ARGUMENT)
+    assert _call_static(lib, batch, max_event_hits=100000)[0] == native.ERR_CAPACITY
+    assert _call_static(lib, batch, y=17)[0] == native.ERR_INVALID_ARGUMENT
     st = lib.velo_search_device_static(None, None, None, native.STATIC_MAX_EVENTS + 1, 0, 100, 4, None, 0,
                                        None, None, None, None)
     assert st == native.ERR_CAPACITY
