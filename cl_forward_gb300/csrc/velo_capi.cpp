@@ -77,6 +77,9 @@ struct velo_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int sm_count = 0;
+  // the device reads and writes pageable host memory coherently through the
+  // host's page tables (a Grace-coupled GPU over NVLink-C2C)
+  bool coherent_host = false;
   int max_smem_optin = 0;
   int l2_bytes = 0;
   std::string err;
@@ -364,6 +367,13 @@ velo_status velo_create(velo_ctx** out, int32_t device) {
   if (e == cudaSuccess)
     e = cudaDeviceGetAttribute(&c->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->l2_bytes, cudaDevAttrL2CacheSize, device);
+  if (e == cudaSuccess) {
+    int pageable = 0, host_tables = 0;
+    e = cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+    if (e == cudaSuccess)
+      e = cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+    c->coherent_host = pageable == 1 && host_tables == 1;
+  }
   if (e == cudaSuccess) e = cudaEventCreate(&c->e0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->e1);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->meta_copied, cudaEventDisableTiming);
@@ -417,7 +427,7 @@ void* device_view(const void* host) {
 }
 
 velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
-                       int32_t n, bool direct);
+                       int32_t n, bool direct, bool pageable = false);
 
 }  // namespace
 
@@ -433,9 +443,11 @@ velo_status velo_stage(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
 namespace {
 
 // Stages a batch: host checks, per-event metadata, and the events themselves
-// (copied, or with `direct` read in place when buf is mapped pinned memory).
+// (copied, or with `direct` read in place when buf is mapped pinned memory;
+// with `pageable` as well, on a device with coherent access to pageable host
+// memory, read in place wherever they are).
 velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
-                       int32_t n, bool direct) {
+                       int32_t n, bool direct, bool pageable) {
   if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
   HostTimer timer(&c->stats.host_stage_ms);
   VELO_CUDA(c, cudaSetDevice(c->device));
@@ -490,6 +502,7 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   c->input_bytes = hi - lo;
   velo_status st;
   if (direct && hi > lo) c->io_input = static_cast<const uint8_t*>(device_view(buf + lo));
+  if (direct && pageable && hi > lo && !c->io_input && c->coherent_host) c->io_input = buf + lo;
   if (!c->io_input && (st = ensure(c, c->d_input, hi - lo + 16, "input")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_offset, 8ull * n, "offsets")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_hits, 4ull * n, "hits")) != VELO_OK) return st;
@@ -647,6 +660,10 @@ velo_status check_options(velo_ctx* c, const velo_options* opts, velo_options* o
     c->err = "register_ctas 18 is the 64-thread build";
     return VELO_ERR_INVALID_ARGUMENT;
   }
+  if (o->learned_min_window < 0) {
+    c->err = "learned_min_window must be >= 0";
+    return VELO_ERR_INVALID_ARGUMENT;
+  }
   if (o->learned && !c->mlp_set) {
     c->err = "learned seeding needs weights (velo_set_mlp)";
     return VELO_ERR_INVALID_ARGUMENT;
@@ -728,6 +745,7 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
     p.window_margin = c->window_margin;
     p.min_keep_rate = c->min_keep_rate;
     p.learned_max_hits = c->learned_max_hits;
+    p.learned_min_window = o.learned_min_window;
   }
   if (c->dump_armed) {
     p.dump_features = P<float>(c->d_dump_features);
@@ -1111,12 +1129,32 @@ velo_status velo_search_packed(velo_ctx* c, const uint8_t* buf, const uint64_t* 
   return VELO_OK;
 }
 
-velo_status velo_search(velo_ctx* c, const uint8_t* const* events, const uint64_t* sizes, int32_t n,
-                        const velo_options* opts, velo_track* tracks_out, uint64_t capacity,
-                        uint32_t* counts, uint64_t* first, uint32_t* status) {
-  if (!c || n < 0 || (n > 0 && (!events || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
-  VELO_CUDA(c, cudaSetDevice(c->device));
-  std::vector<uint64_t> offs(n);
+}  // extern "C"
+
+namespace {
+
+// Runs f(a, b) over [0, n) on up to 16 host threads when `bytes` is large.
+template <class F>
+void host_parallel(int32_t n, uint64_t bytes, F f) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (bytes <= (64ull << 20) || hw <= 1 || n <= 64) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int32_t chunk = (n + (int32_t)hw - 1) / (int32_t)hw;
+  for (unsigned t = 0; t < hw; ++t) {
+    const int32_t a = (int32_t)t * chunk, b = std::min(n, a + chunk);
+    if (a < b) th.emplace_back(f, a, b);
+  }
+  for (auto& t : th) t.join();
+}
+
+// Packs the events into the context's pinned staging buffer at 16-byte
+// aligned offsets (offs_out); returns the buffer, or null on failure.
+uint8_t* gather_pinned(velo_ctx* c, const uint8_t* const* events, const uint64_t* sizes, int32_t n,
+                       std::vector<uint64_t>& offs, uint64_t* total_out) {
+  offs.resize(n);
   uint64_t total = 0;
   for (int32_t e = 0; e < n; ++e) {
     offs[e] = total;
@@ -1127,29 +1165,152 @@ velo_status velo_search(velo_ctx* c, const uint8_t* const* events, const uint64_
     c->h_stage = nullptr;
     c->h_stage_cap = 0;
     const size_t nb = total + total / 4 + 4096;
-    VELO_CUDA(c, cudaHostAlloc(&c->h_stage, nb, cudaHostAllocDefault));
+    const cudaError_t e = cudaHostAlloc(&c->h_stage, nb, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      cuda_fail(c, e, "cudaHostAlloc");
+      c->h_stage = nullptr;
+      return nullptr;
+    }
     c->h_stage_cap = nb;
   }
   uint8_t* stage = static_cast<uint8_t*>(c->h_stage);
-  // pack the events into pinned memory, in parallel for large batches
-  auto pack = [&](int32_t a, int32_t b) {
+  host_parallel(n, total, [&](int32_t a, int32_t b) {
     for (int32_t e = a; e < b; ++e)
       if (events[e] && sizes[e]) std::memcpy(stage + offs[e], events[e], sizes[e]);
-  };
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  if (total > (64ull << 20) && hw > 1 && n > 64) {
-    std::vector<std::thread> th;
-    const int32_t chunk = (n + (int32_t)hw - 1) / (int32_t)hw;
-    for (unsigned t = 0; t < hw; ++t) {
-      const int32_t a = (int32_t)t * chunk, b = std::min(n, a + chunk);
-      if (a < b) th.emplace_back(pack, a, b);
-    }
-    for (auto& t : th) t.join();
-  } else {
-    pack(0, n);
+  });
+  *total_out = total;
+  return stage;
+}
+
+// Offsets of the caller's event buffers from the lowest of them, for a batch
+// the device reads where it lies; false if an event is not 4-byte aligned.
+bool offsets_in_place(const uint8_t* const* events, const uint64_t* sizes, int32_t n, const uint8_t** base,
+                      std::vector<uint64_t>& offs) {
+  uintptr_t lo = ~(uintptr_t)0;
+  for (int32_t e = 0; e < n; ++e) {
+    if (!sizes[e]) continue;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(events[e]);
+    if (!events[e] || (a & 3u)) return false;
+    lo = std::min(lo, a);
   }
+  if (lo == ~(uintptr_t)0) lo = 0;
+  offs.resize(n);
+  for (int32_t e = 0; e < n; ++e)
+    offs[e] = sizes[e] ? (uint64_t)(reinterpret_cast<uintptr_t>(events[e]) - lo) : 0ull;
+  *base = reinterpret_cast<const uint8_t*>(lo);
+  return true;
+}
+
+// One batch read (and with `sort` x-sorted) in place: the events at
+// base + offs[e] are either in the pinned staging buffer or, on a device
+// with coherent access to pageable host memory, in the caller's own
+// buffers.  Tracks go to tracks_out in place when the device can write it.
+velo_status search_in_place(velo_ctx* c, const uint8_t* base, const uint64_t* offs, const uint64_t* sizes,
+                            int32_t n, velo_options o, bool sort, velo_track* tracks_out, uint64_t capacity,
+                            uint32_t* counts, uint64_t* first, uint32_t* status, bool* read_in_place) {
+  o.use_graph = 0;   // the buffers change from call to call
+  c->io_tracks = nullptr;
+  if (tracks_out && capacity) {
+    c->io_tracks = static_cast<velo_track*>(device_view(tracks_out));
+    if (!c->io_tracks && c->coherent_host) c->io_tracks = tracks_out;
+  }
+  c->io_capacity = c->io_tracks ? capacity : 0;
+  c->io_cursor = nullptr;
+  velo_status st = stage_impl(c, base, offs, sizes, n, true, true);
+  *read_in_place = c->io_input != nullptr;
+  if (st == VELO_OK && sort && !*read_in_place) st = VELO_ERR_INVALID_ARGUMENT;   // never: base is readable
+  if (st == VELO_OK && sort) st = velo_sort_staged(c);
+  if (st == VELO_OK) st = velo_run(c, &o);
+  if (st == VELO_OK) st = velo_fetch(c, tracks_out, capacity, counts, first, status);
+  uint64_t bytes = 0;
+  for (int32_t e = 0; e < n; ++e) bytes += sizes[e];
+  c->input_bytes = bytes;
+  c->io_input = nullptr;
+  c->io_tracks = nullptr;
+  c->io_capacity = 0;
+  c->staged = false;   // the batch pointed into the caller's buffers
+  c->ran = false;
+  c->generation++;
+  if (st != VELO_OK) return st;
+  for (int32_t e = 0; e < n; ++e)
+    if (c->h_status[e] & VELO_EVENT_INVALID) {
+      c->err = "event " + std::to_string(e) + " failed validation";
+      return VELO_ERR_INVALID_EVENT;
+    }
+  return VELO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+velo_status velo_search(velo_ctx* c, const uint8_t* const* events, const uint64_t* sizes, int32_t n,
+                        const velo_options* opts, velo_track* tracks_out, uint64_t capacity,
+                        uint32_t* counts, uint64_t* first, uint32_t* status) {
+  if (!c || n < 0 || (n > 0 && (!events || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  std::vector<uint64_t> offs;
+  if (opts && opts->host_direct && opts->pipeline_events <= 0 && c->coherent_host &&
+      budget_part(c, sizes, n, opts->device_budget_mb) == 0) {
+    // the device reads the caller's buffers where they are: no packing
+    const uint8_t* base = nullptr;
+    if (offsets_in_place(events, sizes, n, &base, offs)) {
+      velo_options o;
+      velo_status st = check_options(c, opts, &o);
+      if (st != VELO_OK) return st;
+      bool in_place = false;
+      return search_in_place(c, base, offs.data(), sizes, n, o, false, tracks_out, capacity, counts, first,
+                             status, &in_place);
+    }
+  }
+  uint64_t total = 0;
+  uint8_t* stage = gather_pinned(c, events, sizes, n, offs, &total);
+  if (!stage) return VELO_ERR_OUT_OF_MEMORY;
   return velo_search_packed(c, stage, offs.data(), sizes, n, opts, tracks_out, capacity, counts, first,
                             status);
+}
+
+velo_status velo_sort_search(velo_ctx* c, uint8_t* const* events, const uint64_t* sizes, int32_t n,
+                             const velo_options* opts, velo_track* tracks_out, uint64_t capacity,
+                             uint32_t* counts, uint64_t* first, uint32_t* status) {
+  if (!c || n < 0 || (n > 0 && (!events || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  velo_options o;
+  velo_status st = check_options(c, opts, &o);
+  if (st != VELO_OK) return st;
+  VELO_CUDA(c, cudaSetDevice(c->device));
+  for (int32_t e = 0; e < n; ++e)
+    if (sizes[e] && (!events[e] || (reinterpret_cast<uintptr_t>(events[e]) & 3u))) {
+      c->err = "event " + std::to_string(e) + ": buffer missing or not 4-byte aligned";
+      return VELO_ERR_INVALID_ARGUMENT;
+    }
+  if (budget_part(c, sizes, n, o.device_budget_mb) > 0) {
+    c->err = "batch larger than the device budget: call with fewer events";
+    return VELO_ERR_OUT_OF_MEMORY;
+  }
+  std::vector<uint64_t> offs;
+  bool in_place = false;
+  if (c->coherent_host && o.host_direct) {
+    // sorted and searched where the caller's buffers lie
+    const uint8_t* base = nullptr;
+    offsets_in_place(events, sizes, n, &base, offs);
+    st = search_in_place(c, base, offs.data(), sizes, n, o, true, tracks_out, capacity, counts, first, status,
+                         &in_place);
+    if (in_place || st != VELO_OK) return st;
+  }
+  // packed into pinned memory, sorted and searched there, the sorted bytes
+  // copied back into the caller's buffers
+  uint64_t total = 0;
+  const uint8_t* const* cev = events;
+  uint8_t* stage = gather_pinned(c, cev, sizes, n, offs, &total);
+  if (!stage) return VELO_ERR_OUT_OF_MEMORY;
+  st = search_in_place(c, stage, offs.data(), sizes, n, o, true, tracks_out, capacity, counts, first, status,
+                       &in_place);
+  if (st != VELO_OK && st != VELO_ERR_INVALID_EVENT) return st;
+  host_parallel(n, total, [&](int32_t a, int32_t b) {
+    for (int32_t e = a; e < b; ++e)
+      if (sizes[e]) std::memcpy(events[e], stage + offs[e], sizes[e]);
+  });
+  return st;
 }
 
 velo_status velo_time_runs(velo_ctx* c, const velo_options* opts, int32_t warmup, int32_t iters,
@@ -1262,8 +1423,10 @@ velo_status velo_sort_staged(velo_ctx* c) {
   if (!c) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
   VELO_CUDA(c, cudaSetDevice(c->device));
-  const int e = velo::launch_sort_modules(P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset),
-                                          P<uint32_t>(c->d_ev_valid), c->n, c->stream);
+  // a batch read in place is sorted in place (velo_sort_search)
+  uint8_t* events = c->io_input ? const_cast<uint8_t*>(c->io_input) : P<uint8_t>(c->d_input);
+  const int e = velo::launch_sort_modules(events, P<uint64_t>(c->d_ev_offset), P<uint32_t>(c->d_ev_valid), c->n,
+                                          c->stream);
   if (e != 0) return cuda_fail(c, (cudaError_t)e, "sort kernel launch");
   return VELO_OK;
 }

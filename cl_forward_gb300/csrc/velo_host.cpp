@@ -31,9 +31,6 @@ std::mutex g_call_mutex;   // one search at a time on the shared context (the re
 // pinned track buffer the kernel writes in place, kept between calls
 velo_track* g_tracks = nullptr;
 uint64_t g_tracks_cap = 0;
-// pinned buffer independent_execute gathers the events into
-uint8_t* g_gather = nullptr;
-uint64_t g_gather_cap = 0;
 
 // Runs f(a, b) over [0, n) on the host's cores when n is large.
 template <class F>
@@ -88,52 +85,45 @@ T* pinned(velo_ctx* c, T*& buf, uint64_t& cap, uint64_t count, const char* where
   return buf;
 }
 
-// independent_execute's sort and search of input[a, a + n) on the GPU: the
-// events are gathered into pinned memory, copied to the device, sorted there
-// with the reference's permutation (velo_sort_staged, byte for byte the
-// result of preorder_by_x), searched, and the sorted bytes are written back
-// into the caller's buffers, which the reference sorts in place through
-// const pointers (Tools.cpp:51-63).
+// independent_execute's sort and search of input[a, a + n) on the GPU
+// (velo_sort_search): each module's hits are x-sorted in the caller's
+// buffers with the reference's permutation (velo_sort_staged, byte for byte
+// the result of preorder_by_x, which sorts them in place through const
+// pointers, Tools.cpp:51-63), then searched.  On a GPU with coherent access
+// to pageable host memory (Grace over NVLink-C2C) the device sorts and reads
+// the events where they lie; otherwise they go through pinned memory and the
+// sorted bytes are copied back.  The tracks land in the pinned track buffer.
 void sort_and_search(const std::vector<const std::vector<uint8_t>*>& input, int a, int n,
                      std::vector<std::vector<uint8_t> >& output) {
   if (n <= 0) return;
   velo_ctx* c = context();
   std::lock_guard<std::mutex> call_lock(g_call_mutex);
-  std::vector<const uint8_t*> ptrs(n);
-  std::vector<uint64_t> offs(n), sizes(n);
-  uint64_t total = 0;
+  std::vector<uint8_t*> ptrs(n);
+  std::vector<uint64_t> sizes(n);
   for (int i = 0; i < n; ++i) {
     const std::vector<uint8_t>* v = input[a + i];
-    ptrs[i] = v->empty() ? nullptr : v->data();
+    ptrs[i] = v->empty() ? nullptr : const_cast<uint8_t*>(v->data());
     sizes[i] = v->size();
-    offs[i] = total;
-    total += (sizes[i] + 15u) & ~15ull;
   }
-  uint8_t* buf = pinned(c, g_gather, g_gather_cap, total ? total : 16, "independent_execute");
-  parallel_for((size_t)n, 256, [&](size_t lo, size_t hi) {
-    for (size_t i = lo; i < hi; ++i)
-      if (sizes[i]) std::memcpy(buf + offs[i], ptrs[i], sizes[i]);
-  });
   const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), n);
   velo_track* tracks = pinned(c, g_tracks, g_tracks_cap, cap, "independent_execute");
   std::vector<uint32_t> counts(n), status(n);
   std::vector<uint64_t> first(n);
   velo_options opts;
   velo_default_options(&opts);   // Y = 4, the reference's output configuration
-  velo_status st = velo_stage(c, buf, offs.data(), sizes.data(), n);
-  if (st == VELO_OK) st = velo_sort_staged(c);
-  if (st == VELO_OK) st = velo_run(c, &opts);
-  if (st == VELO_OK) st = velo_fetch(c, tracks, g_tracks_cap, counts.data(), first.data(), status.data());
-  if (st == VELO_OK) st = velo_fetch_staged(c, buf, total);
+  opts.host_direct = 1;
+  velo_status st = velo_sort_search(c, ptrs.data(), sizes.data(), n, &opts, tracks, g_tracks_cap, counts.data(),
+                                    first.data(), status.data());
+  if (st == VELO_ERR_INVALID_EVENT) {
+    for (int i = 0; i < n; ++i)
+      if (status[i] & VELO_EVENT_INVALID) {
+        const std::string what = "event " + std::to_string(a + i) + " failed validation";
+        fail("invokeParallelSearch", VELO_ERR_INVALID_EVENT, what.c_str());
+      }
+  }
   if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
-  for (int i = 0; i < n; ++i)
-    if (status[i] & VELO_EVENT_INVALID) {
-      const std::string what = "event " + std::to_string(a + i) + " failed validation";
-      fail("invokeParallelSearch", VELO_ERR_INVALID_EVENT, what.c_str());
-    }
   parallel_for((size_t)n, 256, [&](size_t lo, size_t hi) {
     for (size_t i = lo; i < hi; ++i) {
-      if (sizes[i]) std::memcpy(const_cast<uint8_t*>(ptrs[i]), buf + offs[i], sizes[i]);
       std::vector<uint8_t>& out = output[a + i];
       out.resize((size_t)counts[i] * sizeof(velo_track));
       if (counts[i]) std::memcpy(out.data(), &tracks[first[i]], out.size());

@@ -135,6 +135,7 @@ struct SearchParams {
   float window_margin;
   float min_keep_rate;
   uint32_t learned_max_hits;      // larger events take the plain method (0 = no limit)
+  int32_t learned_min_window;     // score only doublets with at least this many h2 candidates
 };
 
 // Launches the search kernel (velo_kernels.cu); reg_ctas (4 or 5) picks the

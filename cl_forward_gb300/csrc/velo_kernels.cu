@@ -97,6 +97,7 @@ struct EventView {
   int event;
   const MlpFrag* mlp;       // learned seeding: weights in shared memory
   float keep_threshold, window_margin;
+  int learned_min_window;   // doublets with narrower h2 windows are searched exactly, unscored
   float* dump_features;     // training-data dump
   uint32_t* dump_ids;
   unsigned long long* dump_count;
@@ -590,18 +591,22 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, const
           }
         }
         if constexpr (kMode == kLearned) {
-          if (__any_sync(kFull, cand)) {             // the warp scores its 32 doublets together
-            if (!cand) {
+          // only doublets with a wide exact h2 window are worth scoring
+          const bool score = cand && b - a >= ev.learned_min_window;
+          if (__any_sync(kFull, score)) {            // the warp scores its doublets together
+            if (!score) {
 #pragma unroll
               for (int q = 0; q < kMlpIn; ++q) feat[q] = 0.f;
             }
             float logit, width;
             mlp_eval_warp(*ev.mlp, feat, &logit, &width);
-            keep = cand && logit >= ev.keep_threshold;
-            tol = fminf(kTolerance, fmaxf(width, 0.f) + ev.window_margin);
+            if (score) {
+              keep = logit >= ev.keep_threshold;
+              tol = fminf(kTolerance, fmaxf(width, 0.f) + ev.window_margin);
+            }
           }
-          // keep-rate bookkeeping for the guard
-          const unsigned mc = __ballot_sync(kFull, cand), mk = __ballot_sync(kFull, cand && keep);
+          // keep-rate bookkeeping for the guard: the scored doublets
+          const unsigned mc = __ballot_sync(kFull, score), mk = __ballot_sync(kFull, score && keep);
           if (lane == 0 && mc) {
             atomicAdd(&s.considered, (uint32_t)__popc(mc));
             atomicAdd(&s.kept, (uint32_t)__popc(mk));
@@ -749,6 +754,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
   ev.event = e;
   ev.mlp = mlp_smem;
   ev.keep_threshold = p.keep_threshold;
+  ev.learned_min_window = p.learned_min_window;
   ev.window_margin = p.window_margin;
   ev.dump_features = p.dump_features;
   ev.dump_ids = p.dump_ids;

@@ -46,7 +46,7 @@ EXPORTED = [
     "velo_get_stats", "velo_time_runs", "velo_host_alloc", "velo_host_free", "velo_device_sm_count",
     "velo_search_device_static", "velo_autotune", "velo_set_mlp", "velo_dump_doublets",
     "velo_mlp_train", "velo_mlp_grad", "velo_mlp_forward", "velo_sort_staged", "velo_fetch_staged",
-    "velo_fit_tracks",
+    "velo_fit_tracks", "velo_sort_search",
 ]
 
 FIT_DTYPE = np.dtype([("x0", "<f4"), ("tx", "<f4"), ("y0", "<f4"), ("ty", "<f4"), ("chi2_ndf", "<f4")])
@@ -68,7 +68,8 @@ class Options(ctypes.Structure):
                 ("use_graph", ctypes.c_int32), ("register_ctas", ctypes.c_int32),
                 ("learned", ctypes.c_int32), ("pipeline_events", ctypes.c_int32),
                 ("host_direct", ctypes.c_int32), ("device_budget_mb", ctypes.c_int32),
-                ("seed_lanes", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("seed_lanes", ctypes.c_int32), ("learned_min_window", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 class Stats(ctypes.Structure):
@@ -141,6 +142,7 @@ def load() -> ctypes.CDLL:
     l.velo_sort_staged.argtypes = [vp]
     l.velo_fetch_staged.argtypes = [vp, vp, u64]
     l.velo_fit_tracks.argtypes = [vp, vp, u64]
+    l.velo_sort_search.argtypes = [vp, vp, vp, i32, ctypes.POINTER(Options), vp, u64, vp, vp, vp]
     _lib = l
     return l
 
@@ -226,6 +228,31 @@ class Context:
                                    _p(counts), _p(first), _p(status))
         if not (allow_invalid and st == ERR_INVALID_EVENT):
             self._check(st, "velo_search")
+        out = [tracks[int(first[e]):int(first[e]) + int(counts[e])].copy() for e in range(n)]
+        return out, status[:n].copy()
+
+    def sort_search(self, blobs: Sequence[bytearray], options: Optional[Options] = None,
+                    allow_invalid: bool = False):
+        """velo_sort_search: sorts the events' modules by x in place (the
+        caller's writable buffers, e.g. bytearrays) and searches them.
+        Returns (list of per-event Track arrays, status uint32[n])."""
+        n = len(blobs)
+        arrs = [np.frombuffer(b, np.uint8) for b in blobs]
+        for a in arrs:
+            if len(a) and not a.flags.writeable:
+                raise ValueError("sort_search sorts in place: pass writable buffers")
+        ptrs = (ctypes.c_void_p * max(n, 1))(*[a.ctypes.data if len(a) else 0 for a in arrs])
+        sizes = np.array([len(b) for b in blobs], np.uint64)
+        cap = int(self._lib.velo_track_capacity(ptrs, _p(sizes), n))
+        tracks = np.zeros(max(cap, 1), TRACK_DTYPE)
+        counts = np.zeros(max(n, 1), np.uint32)
+        first = np.zeros(max(n, 1), np.uint64)
+        status = np.zeros(max(n, 1), np.uint32)
+        opts = options or default_options()
+        st = self._lib.velo_sort_search(self._h, ptrs, _p(sizes), n, ctypes.byref(opts), _p(tracks), cap,
+                                        _p(counts), _p(first), _p(status))
+        if not (allow_invalid and st == ERR_INVALID_EVENT):
+            self._check(st, "velo_sort_search")
         out = [tracks[int(first[e]):int(first[e]) + int(counts[e])].copy() for e in range(n)]
         return out, status[:n].copy()
 

@@ -101,8 +101,12 @@ typedef struct velo_options {
                                  buffer are pinned host memory (cudaHostAlloc/cudaHostRegister,
                                  mapped), the kernel reads the events and writes the tracks in
                                  place over the host link instead of staging copies; other
-                                 buffers are copied as usual.  Results are identical; the
-                                 context holds no staged batch afterwards.  0 = off */
+                                 buffers are copied as usual.  velo_search and
+                                 velo_sort_search: the same, and on a device with coherent
+                                 access to pageable host memory (NVLink-C2C) the events are
+                                 read (and sorted) in the caller's own buffers, unpacked.
+                                 Results are identical; the context holds no staged batch
+                                 afterwards.  0 = off */
   int32_t device_budget_mb;   /* velo_search / velo_search_packed: device memory one call may
                                  use; a batch that needs more (about 275 B per hit) is cut into
                                  pipelined parts that fit.  0 = half the free device memory */
@@ -112,7 +116,10 @@ typedef struct velo_options {
                                  warp slides over an h0's h1 candidates (the reference's Y-lanes
                                  per h0, Kernel.cl:435-436, set how many work-items share one
                                  h0).  Results do not depend on it.  0 = automatic */
-  int32_t reserved[3];
+  int32_t learned_min_window; /* learned seeding: only doublets whose exact h2 window holds at
+                                 least this many hits are scored; narrower ones are searched
+                                 exactly (their search costs less than scoring).  0 = score all */
+  int32_t reserved[2];
 } velo_options;
 
 typedef struct velo_stats {
@@ -164,8 +171,27 @@ velo_status velo_search(velo_ctx* ctx, const uint8_t* const* events, const uint6
                         uint64_t track_capacity, uint32_t* counts_out, uint64_t* first_out,
                         uint32_t* event_status_out);
 
-/* Same, for events already packed in one host buffer (event e at
- * buf + offsets[e], 4-byte aligned).  A pinned buffer is copied directly. */
+/*
+ * The standalone path of the reference in one call: sorts each module's hits
+ * by x in the caller's event buffers, in place and with the reference's
+ * permutation (preorder_by_x, Tools.cpp:46-66, which mutates its input the
+ * same way; GpuPixelSearchByTriplet.cpp:19), then searches the sorted
+ * events.  Outputs as for velo_search.  Each event buffer must be 4-byte
+ * aligned.  With opts->host_direct on a device that reads and writes
+ * pageable host memory coherently (cudaDevAttrPageableMemoryAccess and
+ * ...UsesHostPageTables, as a Grace-coupled GPU over NVLink-C2C does), the
+ * device sorts and reads the events where they lie, and writes the tracks
+ * into tracks_out in place; otherwise the events are packed into pinned
+ * memory, sorted and searched there, and the sorted bytes are copied back.
+ * A batch larger than the device budget is refused (VELO_ERR_OUT_OF_MEMORY):
+ * call with fewer events.  Events that fail validation are left unsorted.
+ */
+velo_status velo_sort_search(velo_ctx* ctx, uint8_t* const* events, const uint64_t* sizes, int32_t n_events,
+                             const velo_options* opts, velo_track* tracks_out, uint64_t track_capacity,
+                             uint32_t* counts_out, uint64_t* first_out, uint32_t* event_status_out);
+
+/* Same as velo_search, for events already packed in one host buffer (event e
+ * at buf + offsets[e], 4-byte aligned).  A pinned buffer is copied directly. */
 velo_status velo_search_packed(velo_ctx* ctx, const uint8_t* buf, const uint64_t* offsets,
                                const uint64_t* sizes, int32_t n_events, const velo_options* opts,
                                velo_track* tracks_out, uint64_t track_capacity,

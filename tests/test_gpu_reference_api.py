@@ -118,3 +118,40 @@ def test_reference_entry_points_on_vectors(native_lib, oracle_lib):
     assert len(compared) > 19900
     assert np.array_equal(dig_gp[compared], ohash[compared])
     assert ms[0] > 0 and ms2[0] > 0
+
+
+@pytest.mark.parametrize("direct", [0, 1])
+def test_sort_search_sorts_in_place(gpu_ctx, oracle_lib, direct):
+    """velo_sort_search: the caller's buffers end up sorted byte for byte as
+    the reference's preorder_by_x leaves them (ties included: the fuzz events
+    put several hits at one x), and the tracks are the oracle's.  host_direct
+    1 lets a device with coherent access to pageable memory sort the buffers
+    where they lie; 0 sorts a pinned copy and copies the bytes back."""
+    from cl_forward_gb300 import fuzz, generator, native
+    raw = generator.generate(range(60, 140))[0] + [fuzz.fuzz_event(s, grid=2.0) for s in range(40)]
+    raw += [fuzz.crowded_event(4, 3000, module=30), fuzz.empty_event()]
+    bufs = [bytearray(b) for b in raw]
+    got, status = gpu_ctx.sort_search(bufs, native.default_options(host_direct=direct))
+    want_sorted = [oracle_lib.sort_by_x(b) for b in raw]
+    assert [bytes(b) for b in bufs] == want_sorted
+    want, wst = oracle_lib.search(want_sorted, 4)
+    assert np.array_equal(status & 0x7, wst & 0x7)
+    for e in range(len(raw)):
+        if not (wst[e] & oracle_lib.PARITY_EXCLUDING):
+            assert index_lists(got[e]) == index_lists(want[e]), e
+    # sorting sorted buffers again changes nothing
+    again, _ = gpu_ctx.sort_search(bufs, native.default_options(host_direct=direct))
+    assert [bytes(b) for b in bufs] == want_sorted
+    assert [index_lists(g) for g in again] == [index_lists(g) for g in got]
+
+
+def test_sort_search_rejects_misaligned_buffers(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import generator, native
+    blob = generator.generate([5])[0][0]
+    raw = bytearray(len(blob) + 1)
+    view = np.frombuffer(raw, np.uint8)[1:]
+    view[:] = np.frombuffer(blob, np.uint8)
+    with pytest.raises(native.VeloError) as err:
+        gpu_ctx.sort_search([view], native.default_options(host_direct=1))
+    assert err.value.status == native.ERR_INVALID_ARGUMENT
+    assert bytes(view) == blob                          # untouched
