@@ -301,7 +301,7 @@ const char* velo_status_string(velo_status s) {
     case VELO_ERR_INVALID_EVENT: return "invalid event blob";
     case VELO_ERR_CAPACITY: return "track buffer too small";
     case VELO_ERR_CUDA: return "CUDA error";
-    case VELO_ERR_TIMEOUT: return "device wait timed out";
+    case VELO_ERR_TIMEOUT: return "device wait timed out (reserved)";
     case VELO_ERR_NO_DEVICE: return "no CUDA device";
     case VELO_ERR_OUT_OF_MEMORY: return "out of device memory";
     case VELO_ERR_NOT_STAGED: return "no staged events";

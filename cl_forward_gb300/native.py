@@ -23,7 +23,7 @@ ERR_INVALID_ARGUMENT = -1
 ERR_INVALID_EVENT = -2
 ERR_CAPACITY = -3
 ERR_CUDA = -4
-ERR_TIMEOUT = -5
+ERR_TIMEOUT = -5            # reserved (no entry point returns it)
 ERR_NO_DEVICE = -6
 ERR_OUT_OF_MEMORY = -7
 ERR_NOT_STAGED = -8

@@ -57,7 +57,9 @@ typedef enum velo_status {
   VELO_ERR_INVALID_EVENT = -2,     /* an event blob failed validation (see event status) */
   VELO_ERR_CAPACITY = -3,          /* caller's track buffer too small; counts are valid */
   VELO_ERR_CUDA = -4,              /* CUDA runtime error; see velo_last_error */
-  VELO_ERR_TIMEOUT = -5,           /* a device-side wait gave up (no GPU hang) */
+  VELO_ERR_TIMEOUT = -5,           /* reserved: no kernel here waits on a flag or a peer, so no
+                                      entry point returns it today; kept so that the codes of
+                                      the others stay fixed */
   VELO_ERR_NO_DEVICE = -6,
   VELO_ERR_OUT_OF_MEMORY = -7,
   VELO_ERR_NOT_STAGED = -8         /* velo_run/velo_fetch without staged input */
