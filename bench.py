@@ -87,6 +87,8 @@ def parse_args():
     ap.add_argument("--no-narrow", action="store_true")
     ap.add_argument("--register-ctas", type=int, default=0, choices=[0, 4, 5, 18],
                     help="register build (0: automatic for the thread count)")
+    ap.add_argument("--seed-lanes", type=int, default=0, choices=[0, 8, 16, 32],
+                    help="seeding lanes per h0 (0: the library's automatic width)")
     ap.add_argument("--graph", action="store_true", help="replay launches from a CUDA graph")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the library's default launch configuration instead of the autotuned one")
@@ -721,7 +723,8 @@ def gpu_arm(args, ranks: Ranks):
     mode = CONFIGS[args.config][3] if args.launch is None else (1 if args.launch == "persistent" else 0)
     opts = native.default_options(threads_per_event=args.threads, launch_mode=mode,
                                   smem_hits=args.smem_hits, narrow_windows=0 if args.no_narrow else 1,
-                                  register_ctas=args.register_ctas, use_graph=1 if args.graph else 0)
+                                  register_ctas=args.register_ctas, use_graph=1 if args.graph else 0,
+                                  seed_lanes=args.seed_lanes)
 
     # pinned host input, 16-byte aligned events
     offs = np.zeros(n, np.uint64)
@@ -815,7 +818,9 @@ def gpu_arm(args, ranks: Ranks):
                    "threads_per_event": opts.threads_per_event, "smem_bytes_per_cta": st.smem_bytes_per_cta,
                    "events_in_global_arena": st.events_in_global, "tracks": int(T.sum()),
                    "ms_per_step_samples": [round(x, 4) for x in steps_ms],
-                   "register_ctas": opts.register_ctas, "cuda_graph": bool(opts.use_graph),
+                   "register_ctas": opts.register_ctas,
+                   "seed_lanes": opts.seed_lanes or "automatic (16 when Y divides 16, else 32)",
+                   "cuda_graph": bool(opts.use_graph),
                    "smem_hits_option": opts.smem_hits, "autotuned": tuned,
                    "e2e_chunk_events": chunk, "e2e_pipeline_events": args.e2e_pipeline,
                    "e2e_io": ("H2D / D2H copies" if args.e2e_copies else

@@ -124,9 +124,9 @@ void sort_and_search(const std::vector<const std::vector<uint8_t>*>& input, int 
   if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
   parallel_for((size_t)n, 256, [&](size_t lo, size_t hi) {
     for (size_t i = lo; i < hi; ++i) {
-      std::vector<uint8_t>& out = output[a + i];
-      out.resize((size_t)counts[i] * sizeof(velo_track));
-      if (counts[i]) std::memcpy(out.data(), &tracks[first[i]], out.size());
+      // assign copies the tracks straight in (resize would zero-fill first)
+      const uint8_t* src = reinterpret_cast<const uint8_t*>(tracks + (counts[i] ? first[i] : 0));
+      output[a + i].assign(src, src + (size_t)counts[i] * sizeof(velo_track));
     }
   });
 }
@@ -162,9 +162,8 @@ int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
   if (st != VELO_OK) fail("invokeParallelSearch", st, velo_last_error(c));
   parallel_for((size_t)eventsToProcess, 512, [&](size_t a, size_t b) {
     for (size_t i = a; i < b; ++i) {
-      std::vector<uint8_t>& out = output[startingEvent + i];
-      out.resize((size_t)counts[i] * sizeof(velo_track));
-      if (counts[i]) std::memcpy(out.data(), &tracks[first[i]], out.size());
+      const uint8_t* src = reinterpret_cast<const uint8_t*>(tracks + (counts[i] ? first[i] : 0));
+      output[startingEvent + i].assign(src, src + (size_t)counts[i] * sizeof(velo_track));
     }
   });
   if (g_verbosity >= 3) {

@@ -273,15 +273,27 @@ def test_device_sort_matches_reference_sort(gpu_ctx, oracle_lib, golden):
 
 
 def test_device_sort_of_sorted_crowded_modules(gpu_ctx, oracle_lib):
-    """Sorting events whose modules are already x-sorted changes nothing and
-    takes one pass per module: with 16,383-hit modules the reference's
-    first-element pivots would walk ~1.3e8 steps in one thread each."""
+    """Sorting events a second time gives the reference's sort of the sorted
+    bytes: the same bytes where a module's x values are distinct, and not
+    where they tie (the reference's partition swaps equal neighbours on
+    every pass).  Modules already in strictly increasing order take one pass:
+    with 16,383-hit modules the reference's first-element pivots would walk
+    ~1.3e8 steps in one thread each."""
     import time
     from cl_forward_gb300 import events, fuzz, generator
-    raw = [fuzz.crowded_event(s, 16383, module=m) for s, m in ((1, 38), (2, 39), (3, 20))]
-    raw += generator.generate(range(2100, 2110))[0]
-    want = [oracle_lib.sort_by_x(b) for b in raw]
-    for batch, expect in ((raw, want), (want, want)):
+    distinct = []
+    for s, m in ((1, 38), (2, 39), (3, 20)):
+        ev = events.unpack_event(fuzz.crowded_event(s, 16383, module=m))
+        rng = np.random.Generator(np.random.PCG64(s))          # every x of the event distinct
+        x = np.unique(rng.uniform(-40, 40, 3 * ev.n_hits).astype(np.float32))
+        ev.x[:] = rng.permutation(x)[:ev.n_hits]
+        distinct.append(events.pack_event(ev))
+    ties = [fuzz.crowded_event(4, 3000, module=30)] + [fuzz.fuzz_event(s, grid=2.0) for s in range(6)]
+    raw = distinct + ties + generator.generate(range(2100, 2110))[0]
+    once = [oracle_lib.sort_by_x(b) for b in raw]
+    twice = [oracle_lib.sort_by_x(b) for b in once]
+    assert twice[:3] == once[:3] and twice[3] != once[3]     # distinct x: fixed point; ties: not
+    for batch, expect in ((raw, once), (once, twice), (once[:3], once[:3])):
         buf, offs, sizes = events.pack_events(batch)
         gpu_ctx.stage(buf, offs, sizes)
         gpu_ctx.synchronize()
@@ -292,7 +304,7 @@ def test_device_sort_of_sorted_crowded_modules(gpu_ctx, oracle_lib):
         staged = gpu_ctx.fetch_staged(len(buf))
         got = [bytes(staged[int(o):int(o) + int(n)]) for o, n in zip(offs, sizes)]
         assert got == expect
-    assert dt < 0.1, f"re-sorting sorted events took {dt * 1e3:.1f} ms"
+    assert dt < 0.1, f"re-sorting sorted 16,383-hit modules took {dt * 1e3:.1f} ms"
 
 
 def test_track_fits_match_least_squares(gpu_ctx, oracle_lib):
