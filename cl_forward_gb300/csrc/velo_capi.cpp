@@ -699,7 +699,7 @@ velo_status launch_shape(velo_ctx* c, const velo_options& o, uint32_t smem, int*
     if (per_sm <= 0) {
       int occ = 0;
       int e = velo::search_occupancy(o.threads_per_event, launch_smem(o, smem), o.register_ctas,
-                                     launch_mode_of(c, o), compact_of(c), &occ);
+                                     launch_mode_of(c, o), compact_of(c), o.seed_lanes, &occ);
       if (e != 0) return cuda_fail(c, (cudaError_t)e, "occupancy");
       per_sm = std::max(occ, 1);
     }

@@ -139,7 +139,7 @@ struct SearchParams {
 };
 
 // Launches the search kernel (velo_kernels.cu); reg_ctas (4 or 5) picks the
-// register budget of the <= 256-thread build.  Returns a cudaError_t value.
+// register budget of the <= 256-thread build, p.seed_lanes the seeding width.  Returns a cudaError_t value.
 // compact: every event of the launch has fewer than 64 modules (the compact
 // shared-state build).
 int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_bytes, void* stream, int reg_ctas,
@@ -147,7 +147,8 @@ int launch_search(const SearchParams& p, int grid, int block, uint32_t smem_byte
 // Sets the kernels' maximum dynamic shared memory.  Returns a cudaError_t value.
 int configure_search_kernel(uint32_t smem_bytes);
 // Maximum resident CTAs per SM for a block size, shared-memory size and build.
-int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, bool compact, int* ctas_per_sm);
+int search_occupancy(int block, uint32_t smem_bytes, int reg_ctas, int mode, bool compact, int seed_lanes,
+                     int* ctas_per_sm);
 // Straight-line fits of the compacted output tracks (velo_fit.cu).
 int launch_fit_tracks(const uint8_t* input, const uint64_t* ev_offset, const uint32_t* ev_valid,
                       const velo_track* tracks, const uint32_t* counts, const uint64_t* first, int n_events,
