@@ -1,6 +1,9 @@
 // velo_host.cpp -- the reference's C++ host entry points
 // (GpuPixelSearchByTriplet.cpp:4-65, KernelInvoker.cpp:14-275,
-// Tools.cpp:46-66) on top of the C ABI.
+// Tools.cpp:46-66) on top of the C ABI.  On a GPU with coherent access to
+// host memory (GB300 with Grace) the searches stream their results
+// (velo_search_begin): the host's cores fill the per-event output vectors
+// while the device is still searching.
 //
 // One process-wide context on device 0 (or $VELO_DEVICE) serves these calls,
 // created on first use; like the reference (host globals h_*, Tools.cpp:5-13)
@@ -85,6 +88,66 @@ T* pinned(velo_ctx* c, T*& buf, uint64_t& cap, uint64_t count, const char* where
   return buf;
 }
 
+// Searches (with `sort`, first x-sorts in place) input[a, a + n) with results
+// streamed to the host (velo_search_begin): the host's cores fill each
+// event's output vector as soon as the device has published it, while the
+// search goes on.  Returns false, having started nothing, where the device
+// cannot stream (no coherent access to host memory) or the call was refused;
+// the caller then takes the synchronous path, which reports any error.
+bool streamed_search(velo_ctx* c, std::vector<uint8_t*>& ptrs, std::vector<uint64_t>& sizes, int a, int n,
+                     bool sort, std::vector<std::vector<uint8_t> >& output, const char* where) {
+  const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), n);
+  velo_track* tracks = pinned(c, g_tracks, g_tracks_cap, cap, where);
+  std::vector<velo_event_result> results(n);   // written by the device in place
+  velo_options opts;
+  velo_default_options(&opts);   // Y = 4, the reference's output configuration
+  opts.host_direct = 1;
+  if (velo_search_begin(c, ptrs.data(), sizes.data(), n, &opts, sort ? 1 : 0, tracks, g_tracks_cap,
+                        results.data()) != VELO_OK)
+    return false;
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::seconds(600);
+  std::vector<uint8_t> filled(n, 0);
+  parallel_for((size_t)n, 256, [&](size_t lo, size_t hi) {
+    std::vector<uint32_t> pending;
+    for (size_t i = lo; i < hi; ++i) pending.push_back((uint32_t)i);
+    size_t polls = 0;
+    while (!pending.empty()) {
+      size_t keep = 0;
+      for (uint32_t i : pending) {
+        velo_event_result& r = results[i];
+        if (__atomic_load_n(&r.ready, __ATOMIC_ACQUIRE)) {
+          const uint8_t* src = reinterpret_cast<const uint8_t*>(tracks + (r.count ? r.first : 0));
+          output[a + i].assign(src, src + (size_t)r.count * sizeof(velo_track));
+          filled[i] = 1;
+        } else {
+          pending[keep++] = i;
+        }
+      }
+      if (keep == pending.size()) {
+        std::this_thread::yield();
+        if ((++polls & 1023u) == 0 && std::chrono::steady_clock::now() > deadline) break;
+      }
+      pending.resize(keep);
+    }
+  });
+  std::vector<uint32_t> counts(n), status(n);
+  std::vector<uint64_t> first(n);
+  const velo_status st = velo_search_end(c, counts.data(), first.data(), status.data());
+  if (st == VELO_ERR_INVALID_EVENT)
+    for (int i = 0; i < n; ++i)
+      if (status[i] & VELO_EVENT_INVALID) {
+        const std::string what = "event " + std::to_string(a + i) + " failed validation";
+        fail(where, VELO_ERR_INVALID_EVENT, what.c_str());
+      }
+  if (st != VELO_OK) fail(where, st, velo_last_error(c));
+  for (int i = 0; i < n; ++i)   // events the host stopped waiting for (none, unless the deadline passed)
+    if (!filled[i]) {
+      const uint8_t* src = reinterpret_cast<const uint8_t*>(tracks + (counts[i] ? first[i] : 0));
+      output[a + i].assign(src, src + (size_t)counts[i] * sizeof(velo_track));
+    }
+  return true;
+}
+
 // independent_execute's sort and search of input[a, a + n) on the GPU
 // (velo_sort_search): each module's hits are x-sorted in the caller's
 // buffers with the reference's permutation (velo_sort_staged, byte for byte
@@ -105,6 +168,7 @@ void sort_and_search(const std::vector<const std::vector<uint8_t>*>& input, int 
     ptrs[i] = v->empty() ? nullptr : const_cast<uint8_t*>(v->data());
     sizes[i] = v->size();
   }
+  if (streamed_search(c, ptrs, sizes, a, n, true, output, "independent_execute")) return;
   const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), n);
   velo_track* tracks = pinned(c, g_tracks, g_tracks_cap, cap, "independent_execute");
   std::vector<uint32_t> counts(n), status(n);
@@ -145,6 +209,12 @@ int invokeParallelSearch(const int startingEvent, const int eventsToProcess,
     const std::vector<uint8_t>* v = input[startingEvent + i];
     ptrs[i] = v->empty() ? nullptr : v->data();
     sizes[i] = v->size();
+  }
+  {   // the events are only read (no sort)
+    std::vector<uint8_t*> wptrs(eventsToProcess);
+    for (int i = 0; i < eventsToProcess; ++i) wptrs[i] = const_cast<uint8_t*>(ptrs[i]);
+    if (streamed_search(c, wptrs, sizes, startingEvent, eventsToProcess, false, output, "invokeParallelSearch"))
+      return 0;
   }
   // grow-only, not zero-filled: only [first, first + count) is read
   const uint64_t cap = velo_track_capacity(ptrs.data(), sizes.data(), eventsToProcess);

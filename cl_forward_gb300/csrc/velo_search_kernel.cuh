@@ -757,6 +757,19 @@ static __device__ unsigned long long g_phase_cycles[8];   // one per translation
 #define VELO_PHASE_END() do {} while (0)
 #endif
 
+// Streaming results (velo_search_begin): thread 0 writes the event's record,
+// its ready flag last, after a system-scope fence; the caller has fenced the
+// CTA's track writes before.
+__device__ __forceinline__ void publish_result(const SearchParams& p, int e, unsigned long long first,
+                                               uint32_t count, uint32_t status) {
+  velo_event_result* r = p.results + e;
+  r->first = first;
+  r->count = count;
+  r->status = status;
+  __threadfence_system();
+  *reinterpret_cast<volatile uint32_t*>(&r->ready) = 1u;
+}
+
 // ---------------------------------------------------------------------------
 template <int kMode, int kLanes, class Shared>
 __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* dyn, const MlpFrag* mlp_smem) {
@@ -768,6 +781,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       p.out_counts[e] = 0;
       p.out_first[e] = 0;
       p.out_status[e] = VELO_EVENT_INVALID;
+      if (p.results) publish_result(p, e, 0ull, 0u, VELO_EVENT_INVALID);
     }
     return;
   }
@@ -838,6 +852,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       p.out_counts[e] = 0;
       p.out_first[e] = 0;
       p.out_status[e] = VELO_EVENT_INVALID;
+      if (p.results) publish_result(p, e, 0ull, 0u, VELO_EVENT_INVALID);
     }
     return;
   }
@@ -986,6 +1001,11 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     const uint32_t* src = reinterpret_cast<const uint32_t*>(ev.tracks);
     uint32_t* dst = reinterpret_cast<uint32_t*>(p.out_tracks + s.out_first);
     for (uint32_t w = tid; w < words; w += nt) dst[w] = src[w];
+  }
+  if (p.results) {   // streaming: the tracks first, then the record
+    __threadfence_system();
+    __syncthreads();
+    if (tid == 0) publish_result(p, e, s.out_first, min(s.ntracks, ev.cap), s.status | fallback);
   }
   VELO_PHASE(6);
   VELO_PHASE_END();

@@ -21,6 +21,12 @@
 //    nothing) and is not written;
 //  * a module with a non-finite x is left alone: the reference's sort does
 //    not return on a NaN, and the search marks such an event invalid.
+//
+// For events in the caller's host memory (velo_sort_search on a GPU that
+// reads pageable memory coherently) gather_sort_kernel copies each event
+// into device memory in one pass and sorts it there (the sort's many small
+// dependent accesses are cheap in HBM, not across the host link), and
+// write_back_kernel returns the moved hit arrays in one pass.
 #include <cuda_runtime.h>
 
 #include "velo_internal.h"
@@ -84,12 +90,11 @@ struct SortStage {
   uint32_t id[kSortWarps][kRankMax];
 };
 
-__global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* input, const uint64_t* offsets,
-                                                                    const uint32_t* valid, int n_events) {
-  __shared__ SortStage st;
-  const int e = blockIdx.x;
-  if (e >= n_events || !valid[e]) return;
-  int32_t* hdr = reinterpret_cast<int32_t*>(input + offsets[e]);
+// Sorts the modules of one event in place (all threads of the CTA call it);
+// returns, in every thread, whether any byte moved.  Events whose module
+// table does not tile their hits are left alone.
+__device__ bool sort_event(uint8_t* event, SortStage& st) {
+  int32_t* hdr = reinterpret_cast<int32_t*>(event);
   const int S = hdr[0], H = hdr[1];
   const int32_t* start = hdr + 2 + S;
   const int32_t* num = start + S;
@@ -104,12 +109,13 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
     bad |= num[m] < 0 || num[m] > VELO_MAX_MODULE_HITS || (int64_t)start[m] != expect ||
            (m == S - 1 && (int64_t)start[m] + (int64_t)num[m] != (int64_t)H);
   }
-  if (__syncthreads_or(bad)) return;
+  if (__syncthreads_or(bad)) return false;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float* sx = st.x[w];
   float* sy = st.y[w];
   float* sz = st.z[w];
   uint32_t* sid = st.id[w];
+  bool wrote = false;
   for (int m = w; m < S; m += kSortWarps) {   // warp-uniform
     const int s0 = start[m], n = num[m];
     if (n < 2) continue;
@@ -122,7 +128,10 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
           finite &= isfinite(x[i]) != 0;
           if (i > s0) increasing &= x[i - 1] < x[i];
         }
-        if (finite && !increasing) quicksort4(x, y, z, id, s0, s0 + n - 1);
+        if (finite && !increasing) {
+          quicksort4(x, y, z, id, s0, s0 + n - 1);
+          wrote = true;
+        }
       }
       continue;
     }
@@ -159,11 +168,15 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
     }
     if (__any_sync(kFullMask, tie)) {
       // equal x values: the reference's partition steps decide their order
-      if (lane == 0) quicksort4(x, y, z, id, s0, s0 + n - 1);
+      if (lane == 0) {
+        quicksort4(x, y, z, id, s0, s0 + n - 1);
+        wrote = true;
+      }
       __syncwarp();
       continue;
     }
     if (!__any_sync(kFullMask, moved)) continue;   // strictly increasing already
+    wrote = true;
 #pragma unroll
     for (int k = 0; k < kRankMax / 32; ++k) {
       const int i = lane + 32 * k;
@@ -177,6 +190,55 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
     }
     __syncwarp();   // the staging buffer is refilled for the next module
   }
+  return __syncthreads_or(wrote) != 0;
+}
+
+__global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* input, const uint64_t* offsets,
+                                                                    const uint32_t* valid, int n_events) {
+  __shared__ SortStage st;
+  const int e = blockIdx.x;
+  if (e >= n_events || !valid[e]) return;
+  sort_event(input + offsets[e], st);
+}
+
+// Copies event e from the caller's host memory (src_base + src_off[e], a
+// 4-byte aligned buffer the device reads coherently) into the staged device
+// batch (dst + dst_off[e]) in one pass of 4-byte words, then sorts it there;
+// moved[e] tells whether the sort changed it.
+__global__ void __launch_bounds__(kSortThreads) gather_sort_kernel(const uint8_t* src_base, const uint64_t* src_off,
+                                                                   const uint64_t* sizes, uint8_t* dst,
+                                                                   const uint64_t* dst_off, const uint32_t* valid,
+                                                                   uint32_t* moved, int n_events) {
+  __shared__ SortStage st;
+  const int e = blockIdx.x;
+  if (e >= n_events) return;
+  const uint8_t* src = src_base + src_off[e];
+  uint8_t* out = dst + dst_off[e];
+  const uint64_t size = sizes[e];
+  const uint64_t words = size >> 2;
+  const uint32_t* s4 = reinterpret_cast<const uint32_t*>(src);
+  uint32_t* d4 = reinterpret_cast<uint32_t*>(out);
+  for (uint64_t i = threadIdx.x; i < words; i += blockDim.x) d4[i] = s4[i];
+  if (threadIdx.x < (size & 3u)) out[(words << 2) + threadIdx.x] = src[(words << 2) + threadIdx.x];
+  __syncthreads();
+  const bool m = valid[e] ? sort_event(out, st) : false;
+  if (threadIdx.x == 0) moved[e] = m ? 1u : 0u;
+}
+
+// Writes the sorted hit arrays (IDs, x, y, z: the bytes the sort moves) of
+// every event the sort changed back into the caller's host buffer.
+__global__ void __launch_bounds__(kSortThreads) write_back_kernel(const uint8_t* dst, const uint64_t* dst_off,
+                                                                  uint8_t* src_base, const uint64_t* src_off,
+                                                                  const uint32_t* moved, int n_events) {
+  const int e = blockIdx.x;
+  if (e >= n_events || !moved[e]) return;
+  const uint8_t* in = dst + dst_off[e];
+  const int32_t* hdr = reinterpret_cast<const int32_t*>(in);
+  const uint64_t S = (uint64_t)hdr[0], H = (uint64_t)hdr[1];
+  const uint64_t w0 = 2 + 3 * S, words = 4 * H;   // hit arrays: 4 H words after the header and tables
+  const uint32_t* s4 = reinterpret_cast<const uint32_t*>(in) + w0;
+  uint32_t* d4 = reinterpret_cast<uint32_t*>(src_base + src_off[e]) + w0;
+  for (uint64_t i = threadIdx.x; i < words; i += blockDim.x) d4[i] = s4[i];
 }
 
 }  // namespace
@@ -184,6 +246,22 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
 int launch_sort_modules(uint8_t* input, const uint64_t* offsets, const uint32_t* valid, int n_events, void* stream) {
   if (n_events <= 0) return 0;
   sort_modules_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(input, offsets, valid, n_events);
+  return (int)cudaGetLastError();
+}
+
+int launch_gather_sort(const uint8_t* src_base, const uint64_t* src_off, const uint64_t* sizes, uint8_t* dst,
+                       const uint64_t* dst_off, const uint32_t* valid, uint32_t* moved, int n_events, void* stream) {
+  if (n_events <= 0) return 0;
+  gather_sort_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(src_base, src_off, sizes, dst, dst_off,
+                                                                         valid, moved, n_events);
+  return (int)cudaGetLastError();
+}
+
+int launch_write_back(const uint8_t* dst, const uint64_t* dst_off, uint8_t* src_base, const uint64_t* src_off,
+                      const uint32_t* moved, int n_events, void* stream) {
+  if (n_events <= 0) return 0;
+  write_back_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(dst, dst_off, src_base, src_off, moved,
+                                                                        n_events);
   return (int)cudaGetLastError();
 }
 

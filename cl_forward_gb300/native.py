@@ -46,8 +46,12 @@ EXPORTED = [
     "velo_get_stats", "velo_time_runs", "velo_host_alloc", "velo_host_free", "velo_device_sm_count",
     "velo_search_device_static", "velo_autotune", "velo_set_mlp", "velo_dump_doublets",
     "velo_mlp_train", "velo_mlp_grad", "velo_mlp_forward", "velo_sort_staged", "velo_fetch_staged",
-    "velo_fit_tracks", "velo_sort_search",
+    "velo_fit_tracks", "velo_sort_search", "velo_search_begin", "velo_search_end",
 ]
+
+# velo_event_result (32 bytes)
+RESULT_DTYPE = np.dtype([("first", "<u8"), ("count", "<u4"), ("status", "<u4"), ("ready", "<u4"),
+                         ("reserved", "<u4", 3)])
 
 FIT_DTYPE = np.dtype([("x0", "<f4"), ("tx", "<f4"), ("y0", "<f4"), ("ty", "<f4"), ("chi2_ndf", "<f4")])
 
@@ -143,6 +147,8 @@ def load() -> ctypes.CDLL:
     l.velo_fetch_staged.argtypes = [vp, vp, u64]
     l.velo_fit_tracks.argtypes = [vp, vp, u64]
     l.velo_sort_search.argtypes = [vp, vp, vp, i32, ctypes.POINTER(Options), vp, u64, vp, vp, vp]
+    l.velo_search_begin.argtypes = [vp, vp, vp, i32, ctypes.POINTER(Options), i32, vp, u64, vp]
+    l.velo_search_end.argtypes = [vp, vp, vp, vp]
     _lib = l
     return l
 
@@ -255,6 +261,31 @@ class Context:
             self._check(st, "velo_sort_search")
         out = [tracks[int(first[e]):int(first[e]) + int(counts[e])].copy() for e in range(n)]
         return out, status[:n].copy()
+
+    def search_begin(self, blobs: Sequence[bytearray], sort: bool = False, options: Optional[Options] = None):
+        """velo_search_begin: starts a search whose per-event results the
+        device publishes as events finish.  Returns (results, tracks, keep):
+        the RESULT_DTYPE records and the track buffer the device fills, and
+        the objects to keep alive until :meth:`search_end`."""
+        n = len(blobs)
+        arrs = [np.frombuffer(b, np.uint8) for b in blobs]
+        ptrs = (ctypes.c_void_p * max(n, 1))(*[a.ctypes.data if len(a) else 0 for a in arrs])
+        sizes = np.array([len(b) for b in blobs], np.uint64)
+        cap = int(self._lib.velo_track_capacity(ptrs, _p(sizes), n))
+        tracks = np.zeros(max(cap, 1), TRACK_DTYPE)
+        results = np.zeros(max(n, 1), RESULT_DTYPE)
+        opts = options or default_options(host_direct=1)
+        st = self._lib.velo_search_begin(self._h, ptrs, _p(sizes), n, ctypes.byref(opts), int(sort), _p(tracks),
+                                         cap, _p(results))
+        self._check(st, "velo_search_begin")
+        return results[:n], tracks, (arrs, ptrs, sizes, opts)
+
+    def search_end(self, n_events: int):
+        counts = np.zeros(max(n_events, 1), np.uint32)
+        first = np.zeros(max(n_events, 1), np.uint64)
+        status = np.zeros(max(n_events, 1), np.uint32)
+        self._check(self._lib.velo_search_end(self._h, _p(counts), _p(first), _p(status)), "velo_search_end")
+        return counts[:n_events], first[:n_events], status[:n_events]
 
     # -- split path ----------------------------------------------------------
     def stage(self, buf: np.ndarray, offsets: np.ndarray, sizes: np.ndarray):

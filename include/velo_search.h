@@ -192,6 +192,39 @@ velo_status velo_sort_search(velo_ctx* ctx, uint8_t* const* events, const uint64
                              const velo_options* opts, velo_track* tracks_out, uint64_t track_capacity,
                              uint32_t* counts_out, uint64_t* first_out, uint32_t* event_status_out);
 
+/*
+ * Streaming form, for a host that consumes events while the device is still
+ * searching (it hides the host's per-event work behind the search).  It
+ * needs a device that reads and writes pageable host memory coherently
+ * (NVLink-C2C); elsewhere velo_search_begin returns VELO_ERR_INVALID_ARGUMENT
+ * and nothing starts.  No counterpart in the reference, whose host waits for
+ * the whole launch (KernelInvoker.cpp:197-206).
+ *
+ * velo_search_begin enqueues the search (with sort != 0 after the in-place
+ * sort of velo_sort_search, events 4-byte aligned) and returns.  As each
+ * event finishes, the device writes its tracks to tracks_out and then its
+ * record results[e]; `ready` is written last, after a system-scope fence,
+ * so a host thread that reads ready == 1 (with acquire ordering) may read
+ * the record and the event's tracks.  tracks_out and results stay the
+ * caller's and must not be touched by it before velo_search_end except to
+ * read finished events; track_capacity must be at least
+ * velo_track_capacity() of the batch.  velo_search_end waits for the
+ * search (and the sort's write-back) and returns the per-event outputs and
+ * the status of velo_search.
+ */
+typedef struct velo_event_result {
+  uint64_t first;        /* first track of the event in tracks_out */
+  uint32_t count;        /* its tracks */
+  uint32_t status;       /* VELO_EVENT_* bits */
+  uint32_t ready;        /* set to 1 by the device, last */
+  uint32_t reserved[3];
+} velo_event_result;
+velo_status velo_search_begin(velo_ctx* ctx, uint8_t* const* events, const uint64_t* sizes, int32_t n_events,
+                              const velo_options* opts, int32_t sort, velo_track* tracks_out,
+                              uint64_t track_capacity, velo_event_result* results);
+velo_status velo_search_end(velo_ctx* ctx, uint32_t* counts_out, uint64_t* first_out,
+                            uint32_t* event_status_out);
+
 /* Same as velo_search, for events already packed in one host buffer (event e
  * at buf + offsets[e], 4-byte aligned).  A pinned buffer is copied directly. */
 velo_status velo_search_packed(velo_ctx* ctx, const uint8_t* buf, const uint64_t* offsets,

@@ -160,3 +160,50 @@ def test_sort_search_rejects_misaligned_buffers(gpu_ctx, oracle_lib):
         gpu_ctx.sort_search([view], native.default_options(host_direct=1))
     assert err.value.status == native.ERR_INVALID_ARGUMENT
     assert bytes(view) == blob                          # untouched
+
+
+@pytest.mark.parametrize("sort", [0, 1])
+def test_streamed_results(gpu_ctx, oracle_lib, sort):
+    """velo_search_begin / velo_search_end: every event's record becomes ready
+    while or after the device searches, its tracks are in place once it is,
+    and records, tracks and the end call's outputs equal the synchronous
+    search's (with sort, after the in-place sort of the caller's buffers)."""
+    import time
+    from cl_forward_gb300 import fuzz, generator, native
+    raw = generator.generate(range(200, 500))[0] + [fuzz.fuzz_event(s, grid=2.0) for s in range(20)]
+    raw += [fuzz.empty_event()]
+    want_sorted = [oracle_lib.sort_by_x(b) for b in raw]
+    bufs = [bytearray(b) for b in (raw if sort else want_sorted)]
+    results, tracks, keep = gpu_ctx.search_begin(bufs, sort=bool(sort))
+    t0 = time.perf_counter()
+    while not results["ready"].all():
+        assert time.perf_counter() - t0 < 60, "records not ready"
+        time.sleep(0.0005)
+    got = [tracks[int(r["first"]):int(r["first"]) + int(r["count"])].copy() for r in results]
+    counts, first, status = gpu_ctx.search_end(len(bufs))
+    assert np.array_equal(counts, results["count"]) and np.array_equal(first, results["first"])
+    assert np.array_equal(status, results["status"])
+    assert [bytes(b) for b in bufs] == want_sorted
+    want, wst = oracle_lib.search(want_sorted, 4)
+    assert np.array_equal(status & 0x7, wst & 0x7)
+    for e in range(len(raw)):
+        if not (wst[e] & oracle_lib.PARITY_EXCLUDING):
+            assert index_lists(got[e]) == index_lists(want[e]), e
+    del keep
+
+
+def test_streamed_search_call_order(gpu_ctx, oracle_lib):
+    from cl_forward_gb300 import generator, native
+    bufs = [bytearray(oracle_lib.sort_by_x(b)) for b in generator.generate(range(600, 610))[0]]
+    with pytest.raises(native.VeloError) as err:
+        gpu_ctx.search_end(len(bufs))                       # nothing in flight
+    assert err.value.status == native.ERR_NOT_STAGED
+    results, tracks, keep = gpu_ctx.search_begin(bufs)
+    with pytest.raises(native.VeloError) as err:
+        gpu_ctx.search_begin(bufs)                          # one streamed search at a time
+    assert err.value.status == native.ERR_INVALID_ARGUMENT
+    counts, _, _ = gpu_ctx.search_end(len(bufs))
+    assert results["ready"].all() and np.array_equal(counts, results["count"])
+    got, _ = gpu_ctx.search(bufs)                            # the context works on
+    assert [len(g) for g in got] == counts.tolist()
+    del keep
