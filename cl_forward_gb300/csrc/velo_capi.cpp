@@ -133,16 +133,12 @@ struct velo_ctx {
   unsigned long long* io_cursor = nullptr;   // output cursor shared by pipelined parts
 
   // velo_sort_search on a coherent host: source offsets and sizes of the
-  // events in the caller's memory, the sort's per-event "moved" flags, and a
-  // side stream for writing the sorted bytes back while the search runs
+  // events in the caller's memory
   PinnedVec<uint64_t> h_src_offset, h_sizes;
-  DevBuf d_src_offset, d_sizes, d_moved;
-  cudaStream_t side = nullptr;
-  cudaEvent_t sorted_ev = nullptr, written_ev = nullptr;
+  DevBuf d_src_offset, d_sizes;
   // streamed search in flight (velo_search_begin .. velo_search_end)
   velo_event_result* io_results = nullptr;
   bool streaming = false;
-  bool stream_sorted = false;
 
   // pipelined searches (velo_options.pipeline_events): two child contexts,
   // each with its own stream and buffers, that alternate over the parts
@@ -407,8 +403,7 @@ void velo_destroy(velo_ctx* c) {
                     &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_rings, &c->d_weak,
                     &c->d_tracks, &c->d_out_tracks, &c->d_out_counts, &c->d_out_first,
                     &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush, &c->d_mlp,
-                    &c->d_dump_features, &c->d_dump_ids, &c->d_fits, &c->d_src_offset, &c->d_sizes,
-                    &c->d_moved};
+                    &c->d_dump_features, &c->d_dump_ids, &c->d_fits, &c->d_src_offset, &c->d_sizes};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -416,12 +411,6 @@ void velo_destroy(velo_ctx* c) {
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
   if (c->meta_copied) cudaEventDestroy(c->meta_copied);
-  if (c->sorted_ev) cudaEventDestroy(c->sorted_ev);
-  if (c->written_ev) cudaEventDestroy(c->written_ev);
-  if (c->side) {
-    cudaStreamSynchronize(c->side);
-    cudaStreamDestroy(c->side);
-  }
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1275,18 +1264,12 @@ uint64_t packed_offsets(const uint64_t* sizes, int32_t n, std::vector<uint64_t>&
 }
 
 // After stage_impl with dev_offsets: one kernel copies every event from the
-// caller's buffer (base + src_offs[e]) into device memory and sorts it
-// there; a second one, on the side stream, writes the hit arrays the sort
-// moved back into the caller's buffer (written_ev), while the search runs
-// on the device copy.
+// caller's buffer (base + src_offs[e]) into device memory, sorts it there
+// and writes the modules the sort changed back into the caller's buffer;
+// the search then runs on the device copy.
 velo_status enqueue_gather_sort(velo_ctx* c, uint8_t* base, const uint64_t* src_offs, const uint64_t* sizes,
                                 int32_t n) {
   if (n <= 0) return VELO_OK;
-  if (!c->side) {
-    VELO_CUDA(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-    VELO_CUDA(c, cudaEventCreateWithFlags(&c->sorted_ev, cudaEventDisableTiming));
-    VELO_CUDA(c, cudaEventCreateWithFlags(&c->written_ev, cudaEventDisableTiming));
-  }
   // the previous batch's copies out of these pinned arrays are done
   // (stage_impl waited for meta_copied, recorded after them)
   if (!c->h_src_offset.assign(n, 0) || !c->h_sizes.assign(n, 0)) return VELO_ERR_OUT_OF_MEMORY;
@@ -1295,21 +1278,14 @@ velo_status enqueue_gather_sort(velo_ctx* c, uint8_t* base, const uint64_t* src_
   velo_status st;
   if ((st = ensure(c, c->d_src_offset, 8ull * n, "source offsets")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_sizes, 8ull * n, "sizes")) != VELO_OK) return st;
-  if ((st = ensure(c, c->d_moved, 4ull * n, "moved")) != VELO_OK) return st;
   VELO_CUDA(c, cudaMemcpyAsync(c->d_src_offset.p, c->h_src_offset.data(), 8ull * n, cudaMemcpyHostToDevice,
                                c->stream));
   VELO_CUDA(c, cudaMemcpyAsync(c->d_sizes.p, c->h_sizes.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
   VELO_CUDA(c, cudaEventRecord(c->meta_copied, c->stream));
-  int e = velo::launch_gather_sort(base, P<uint64_t>(c->d_src_offset), P<uint64_t>(c->d_sizes),
-                                   P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset), P<uint32_t>(c->d_ev_valid),
-                                   P<uint32_t>(c->d_moved), n, c->stream);
+  const int e = velo::launch_gather_sort(base, P<uint64_t>(c->d_src_offset), P<uint64_t>(c->d_sizes),
+                                         P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset),
+                                         P<uint32_t>(c->d_ev_valid), n, c->stream);
   if (e != 0) return cuda_fail(c, (cudaError_t)e, "gather-sort kernel launch");
-  VELO_CUDA(c, cudaEventRecord(c->sorted_ev, c->stream));
-  VELO_CUDA(c, cudaStreamWaitEvent(c->side, c->sorted_ev, 0));
-  e = velo::launch_write_back(P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset), base, P<uint64_t>(c->d_src_offset),
-                              P<uint32_t>(c->d_moved), n, c->side);
-  if (e != 0) return cuda_fail(c, (cudaError_t)e, "write-back kernel launch");
-  VELO_CUDA(c, cudaEventRecord(c->written_ev, c->side));
   return VELO_OK;
 }
 
@@ -1349,11 +1325,9 @@ velo_status sort_search_gathered(velo_ctx* c, uint8_t* base, const uint64_t* src
   if (st == VELO_OK) st = enqueue_gather_sort(c, base, src_offs, sizes, n);
   if (st != VELO_OK) return end_in_place(c, st);
   st = velo_run(c, &o);
+  // velo_fetch synchronises the stream: the sort's writes into the caller's
+  // buffers are complete too
   if (st == VELO_OK) st = velo_fetch(c, tracks_out, capacity, counts, first, status);
-  if (n > 0) {
-    const cudaError_t we = cudaEventSynchronize(c->written_ev);   // the caller's buffers hold the sorted bytes
-    if (st == VELO_OK && we != cudaSuccess) st = cuda_fail(c, we, "write-back");
-  }
   if (st != VELO_OK) return end_in_place(c, st);
   for (int32_t e = 0; e < n; ++e)
     if (c->h_status[e] & VELO_EVENT_INVALID) {
@@ -1484,22 +1458,16 @@ velo_status velo_search_begin(velo_ctx* c, uint8_t* const* events, const uint64_
   st = velo_run(c, &o);
   if (st != VELO_OK) {
     cudaStreamSynchronize(c->stream);
-    if (c->side) cudaStreamSynchronize(c->side);
     return end_in_place(c, st);
   }
   c->streaming = true;
-  c->stream_sorted = sort != 0 && n > 0;
   return VELO_OK;
 }
 
 velo_status velo_search_end(velo_ctx* c, uint32_t* counts, uint64_t* first, uint32_t* status) {
   if (!c) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->streaming) return VELO_ERR_NOT_STAGED;
-  velo_status st = velo_fetch(c, nullptr, 0, counts, first, status);
-  if (c->stream_sorted) {
-    const cudaError_t we = cudaEventSynchronize(c->written_ev);
-    if (st == VELO_OK && we != cudaSuccess) st = cuda_fail(c, we, "write-back");
-  }
+  velo_status st = velo_fetch(c, nullptr, 0, counts, first, status);   // waits for the sort and the search
   if (st == VELO_OK)
     for (int32_t e = 0; e < c->n; ++e)
       if (c->h_status[e] & VELO_EVENT_INVALID) {

@@ -25,8 +25,8 @@
 // For events in the caller's host memory (velo_sort_search on a GPU that
 // reads pageable memory coherently) gather_sort_kernel copies each event
 // into device memory in one pass and sorts it there (the sort's many small
-// dependent accesses are cheap in HBM, not across the host link), and
-// write_back_kernel returns the moved hit arrays in one pass.
+// dependent accesses are cheap in HBM, not across the host link), writing
+// each module it changes back into the caller's buffer as it goes.
 #include <cuda_runtime.h>
 
 #include "velo_internal.h"
@@ -90,10 +90,25 @@ struct SortStage {
   uint32_t id[kSortWarps][kRankMax];
 };
 
+// Copies hits [s0, s0 + n) of the four hit arrays of a module to the same
+// places of `mirror` (lanes of one warp).
+__device__ __forceinline__ void mirror_module(const float* x, const float* y, const float* z, const uint32_t* id,
+                                              float* mx, float* my, float* mz, uint32_t* mid, int s0, int n,
+                                              int lane) {
+  for (int i = s0 + lane; i < s0 + n; i += 32) {
+    mx[i] = x[i];
+    my[i] = y[i];
+    mz[i] = z[i];
+    mid[i] = id[i];
+  }
+}
+
 // Sorts the modules of one event in place (all threads of the CTA call it);
 // returns, in every thread, whether any byte moved.  Events whose module
-// table does not tile their hits are left alone.
-__device__ bool sort_event(uint8_t* event, SortStage& st) {
+// table does not tile their hits are left alone.  With `mirror` (an event of
+// the same layout: the caller's host copy), every module the sort changes is
+// also written there.
+__device__ bool sort_event(uint8_t* event, SortStage& st, uint8_t* mirror = nullptr) {
   int32_t* hdr = reinterpret_cast<int32_t*>(event);
   const int S = hdr[0], H = hdr[1];
   const int32_t* start = hdr + 2 + S;
@@ -102,6 +117,11 @@ __device__ bool sort_event(uint8_t* event, SortStage& st) {
   float* x = reinterpret_cast<float*>(id + H);
   float* y = x + H;
   float* z = y + H;
+  // the same arrays in the mirror (unused without one)
+  uint32_t* mid = mirror ? reinterpret_cast<uint32_t*>(mirror) + (2 + 3 * S) : nullptr;
+  float* mx = mirror ? reinterpret_cast<float*>(mid + H) : nullptr;
+  float* my = mirror ? mx + H : nullptr;
+  float* mz = mirror ? my + H : nullptr;
   // the module table must tile [0, H) in order before anything moves
   bool bad = threadIdx.x == 0 && S == 0 && H != 0;
   for (int m = threadIdx.x; m < S; m += blockDim.x) {
@@ -122,6 +142,7 @@ __device__ bool sort_event(uint8_t* event, SortStage& st) {
     if (n > kRankMax) {
       // large module: one thread checks it and, unless it is in order
       // already or holds a non-finite x, replays the reference's partitions
+      bool changed = false;
       if (lane == 0) {
         bool finite = true, increasing = true;
         for (int i = s0; i < s0 + n; ++i) {
@@ -130,8 +151,13 @@ __device__ bool sort_event(uint8_t* event, SortStage& st) {
         }
         if (finite && !increasing) {
           quicksort4(x, y, z, id, s0, s0 + n - 1);
-          wrote = true;
+          changed = true;
         }
+      }
+      wrote |= changed;
+      if (mirror) {
+        __syncwarp();
+        if (__shfl_sync(kFullMask, changed, 0)) mirror_module(x, y, z, id, mx, my, mz, mid, s0, n, lane);
       }
       continue;
     }
@@ -173,6 +199,7 @@ __device__ bool sort_event(uint8_t* event, SortStage& st) {
         wrote = true;
       }
       __syncwarp();
+      if (mirror) mirror_module(x, y, z, id, mx, my, mz, mid, s0, n, lane);
       continue;
     }
     if (!__any_sync(kFullMask, moved)) continue;   // strictly increasing already
@@ -186,6 +213,12 @@ __device__ bool sort_event(uint8_t* event, SortStage& st) {
         y[r] = sy[i];
         z[r] = sz[i];
         id[r] = sid[i];
+        if (mirror) {   // posted writes across the host link
+          mx[r] = sx[i];
+          my[r] = sy[i];
+          mz[r] = sz[i];
+          mid[r] = sid[i];
+        }
       }
     }
     __syncwarp();   // the staging buffer is refilled for the next module
@@ -203,42 +236,43 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
 
 // Copies event e from the caller's host memory (src_base + src_off[e], a
 // 4-byte aligned buffer the device reads coherently) into the staged device
-// batch (dst + dst_off[e]) in one pass of 4-byte words, then sorts it there;
-// moved[e] tells whether the sort changed it.
-__global__ void __launch_bounds__(kSortThreads) gather_sort_kernel(const uint8_t* src_base, const uint64_t* src_off,
+// batch (dst + dst_off[e], 16-byte aligned) in one pass, then sorts it there
+// and writes every module the sort changed back into the caller's buffer.
+__global__ void __launch_bounds__(kSortThreads) gather_sort_kernel(uint8_t* src_base, const uint64_t* src_off,
                                                                    const uint64_t* sizes, uint8_t* dst,
                                                                    const uint64_t* dst_off, const uint32_t* valid,
-                                                                   uint32_t* moved, int n_events) {
+                                                                   int n_events) {
   __shared__ SortStage st;
   const int e = blockIdx.x;
   if (e >= n_events) return;
-  const uint8_t* src = src_base + src_off[e];
-  uint8_t* out = dst + dst_off[e];
+  uint8_t* src = src_base + src_off[e];
+  uint8_t* __restrict__ out = dst + dst_off[e];
   const uint64_t size = sizes[e];
-  const uint64_t words = size >> 2;
-  const uint32_t* s4 = reinterpret_cast<const uint32_t*>(src);
-  uint32_t* d4 = reinterpret_cast<uint32_t*>(out);
-  for (uint64_t i = threadIdx.x; i < words; i += blockDim.x) d4[i] = s4[i];
-  if (threadIdx.x < (size & 3u)) out[(words << 2) + threadIdx.x] = src[(words << 2) + threadIdx.x];
+  uint64_t done = 0;
+  if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {   // 16-byte words, four in flight per thread
+    const uint64_t n16 = size >> 4;
+    const uint4* __restrict__ s16 = reinterpret_cast<const uint4*>(src);
+    uint4* __restrict__ d16 = reinterpret_cast<uint4*>(out);
+    uint64_t i = threadIdx.x;
+    for (; i + 3 * kSortThreads < n16; i += 4 * kSortThreads) {
+      const uint4 a = s16[i], b = s16[i + kSortThreads], c = s16[i + 2 * kSortThreads],
+                  d = s16[i + 3 * kSortThreads];
+      d16[i] = a;
+      d16[i + kSortThreads] = b;
+      d16[i + 2 * kSortThreads] = c;
+      d16[i + 3 * kSortThreads] = d;
+    }
+    for (; i < n16; i += kSortThreads) d16[i] = s16[i];
+    done = n16 << 4;
+  }
+  const uint64_t words = (size - done) >> 2;
+  const uint32_t* __restrict__ s4 = reinterpret_cast<const uint32_t*>(src + done);
+  uint32_t* __restrict__ d4 = reinterpret_cast<uint32_t*>(out + done);
+  for (uint64_t i = threadIdx.x; i < words; i += kSortThreads) d4[i] = s4[i];
+  const uint64_t tail = done + (words << 2);
+  if (threadIdx.x < size - tail) out[tail + threadIdx.x] = src[tail + threadIdx.x];
   __syncthreads();
-  const bool m = valid[e] ? sort_event(out, st) : false;
-  if (threadIdx.x == 0) moved[e] = m ? 1u : 0u;
-}
-
-// Writes the sorted hit arrays (IDs, x, y, z: the bytes the sort moves) of
-// every event the sort changed back into the caller's host buffer.
-__global__ void __launch_bounds__(kSortThreads) write_back_kernel(const uint8_t* dst, const uint64_t* dst_off,
-                                                                  uint8_t* src_base, const uint64_t* src_off,
-                                                                  const uint32_t* moved, int n_events) {
-  const int e = blockIdx.x;
-  if (e >= n_events || !moved[e]) return;
-  const uint8_t* in = dst + dst_off[e];
-  const int32_t* hdr = reinterpret_cast<const int32_t*>(in);
-  const uint64_t S = (uint64_t)hdr[0], H = (uint64_t)hdr[1];
-  const uint64_t w0 = 2 + 3 * S, words = 4 * H;   // hit arrays: 4 H words after the header and tables
-  const uint32_t* s4 = reinterpret_cast<const uint32_t*>(in) + w0;
-  uint32_t* d4 = reinterpret_cast<uint32_t*>(src_base + src_off[e]) + w0;
-  for (uint64_t i = threadIdx.x; i < words; i += blockDim.x) d4[i] = s4[i];
+  if (valid[e]) sort_event(out, st, src);
 }
 
 }  // namespace
@@ -249,19 +283,11 @@ int launch_sort_modules(uint8_t* input, const uint64_t* offsets, const uint32_t*
   return (int)cudaGetLastError();
 }
 
-int launch_gather_sort(const uint8_t* src_base, const uint64_t* src_off, const uint64_t* sizes, uint8_t* dst,
-                       const uint64_t* dst_off, const uint32_t* valid, uint32_t* moved, int n_events, void* stream) {
+int launch_gather_sort(uint8_t* src_base, const uint64_t* src_off, const uint64_t* sizes, uint8_t* dst,
+                       const uint64_t* dst_off, const uint32_t* valid, int n_events, void* stream) {
   if (n_events <= 0) return 0;
   gather_sort_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(src_base, src_off, sizes, dst, dst_off,
-                                                                         valid, moved, n_events);
-  return (int)cudaGetLastError();
-}
-
-int launch_write_back(const uint8_t* dst, const uint64_t* dst_off, uint8_t* src_base, const uint64_t* src_off,
-                      const uint32_t* moved, int n_events, void* stream) {
-  if (n_events <= 0) return 0;
-  write_back_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(dst, dst_off, src_base, src_off, moved,
-                                                                        n_events);
+                                                                         valid, n_events);
   return (int)cudaGetLastError();
 }
 
