@@ -135,7 +135,10 @@ struct velo_ctx {
   // velo_sort_search on a coherent host: source offsets and sizes of the
   // events in the caller's memory
   PinnedVec<uint64_t> h_src_offset, h_sizes;
-  DevBuf d_src_offset, d_sizes;
+  DevBuf d_src_offset, d_sizes, d_moved;
+  // the batch was gathered from the caller's buffers (base): the search
+  // writes the sorted hit arrays back there
+  uint8_t* mirror_base = nullptr;
   // streamed search in flight (velo_search_begin .. velo_search_end)
   velo_event_result* io_results = nullptr;
   bool streaming = false;
@@ -403,7 +406,8 @@ void velo_destroy(velo_ctx* c) {
                     &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_rings, &c->d_weak,
                     &c->d_tracks, &c->d_out_tracks, &c->d_out_counts, &c->d_out_first,
                     &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush, &c->d_mlp,
-                    &c->d_dump_features, &c->d_dump_ids, &c->d_fits, &c->d_src_offset, &c->d_sizes};
+                    &c->d_dump_features, &c->d_dump_ids, &c->d_fits, &c->d_src_offset, &c->d_sizes,
+                    &c->d_moved};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -750,6 +754,11 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
   p.out_status = P<uint32_t>(c->d_out_status);
   p.out_cursor = c->io_cursor ? c->io_cursor : P<unsigned long long>(c->d_counters);
   p.results = c->io_results;
+  if (c->mirror_base) {
+    p.mirror_base = c->mirror_base;
+    p.mirror_offset = P<uint64_t>(c->d_src_offset);
+    p.mirror_moved = P<uint32_t>(c->d_moved);
+  }
   p.work_counter = reinterpret_cast<int32_t*>(P<uint8_t>(c->d_counters) + 32);
   if (o.learned) {
     p.mlp = P<float>(c->d_mlp);
@@ -1264,9 +1273,10 @@ uint64_t packed_offsets(const uint64_t* sizes, int32_t n, std::vector<uint64_t>&
 }
 
 // After stage_impl with dev_offsets: one kernel copies every event from the
-// caller's buffer (base + src_offs[e]) into device memory, sorts it there
-// and writes the modules the sort changed back into the caller's buffer;
-// the search then runs on the device copy.
+// caller's buffer (base + src_offs[e]) into device memory and sorts it
+// there; the search then runs on the device copy and, while it stages each
+// event, writes the hit arrays the sort changed back into the caller's
+// buffer (mirror_base), hidden behind the search.
 velo_status enqueue_gather_sort(velo_ctx* c, uint8_t* base, const uint64_t* src_offs, const uint64_t* sizes,
                                 int32_t n) {
   if (n <= 0) return VELO_OK;
@@ -1278,14 +1288,16 @@ velo_status enqueue_gather_sort(velo_ctx* c, uint8_t* base, const uint64_t* src_
   velo_status st;
   if ((st = ensure(c, c->d_src_offset, 8ull * n, "source offsets")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_sizes, 8ull * n, "sizes")) != VELO_OK) return st;
+  if ((st = ensure(c, c->d_moved, 4ull * n, "moved")) != VELO_OK) return st;
   VELO_CUDA(c, cudaMemcpyAsync(c->d_src_offset.p, c->h_src_offset.data(), 8ull * n, cudaMemcpyHostToDevice,
                                c->stream));
   VELO_CUDA(c, cudaMemcpyAsync(c->d_sizes.p, c->h_sizes.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
   VELO_CUDA(c, cudaEventRecord(c->meta_copied, c->stream));
   const int e = velo::launch_gather_sort(base, P<uint64_t>(c->d_src_offset), P<uint64_t>(c->d_sizes),
                                          P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset),
-                                         P<uint32_t>(c->d_ev_valid), n, c->stream);
+                                         P<uint32_t>(c->d_ev_valid), P<uint32_t>(c->d_moved), n, c->stream);
   if (e != 0) return cuda_fail(c, (cudaError_t)e, "gather-sort kernel launch");
+  c->mirror_base = base;
   return VELO_OK;
 }
 
@@ -1303,6 +1315,7 @@ velo_status end_in_place(velo_ctx* c, velo_status r) {
   c->io_tracks = nullptr;
   c->io_capacity = 0;
   c->io_results = nullptr;
+  c->mirror_base = nullptr;
   c->streaming = false;
   c->staged = false;
   c->ran = false;

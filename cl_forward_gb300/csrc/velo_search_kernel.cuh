@@ -834,6 +834,14 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     s.num[m] = nm;
     s.sz[m] = gZ[m];
   }
+  if (p.mirror_base && p.mirror_moved[e]) {
+    // the sorted hit arrays (IDs, x, y, z) back into the caller's buffer,
+    // which this batch was gathered from: posted writes across the host
+    // link, overlapped with the search of this and the other resident events
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(gnum + S);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(p.mirror_base + p.mirror_offset[e]) + (2 + 3 * S);
+    for (int w = tid; w < 4 * H; w += nt) dst[w] = src[w];
+  }
   for (int i = tid; i < H; i += nt) {
     const float xv = gx[i], yv = gy[i], zv = gz[i];
     bad |= !(isfinite(xv) && isfinite(yv) && isfinite(zv));
@@ -1014,9 +1022,11 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
 // Builds: up to 256 threads per CTA with registers budgeted for 4 or for 5
 // resident 256-thread CTAs per SM (velo_options.register_ctas 4 / 5: 64 / 48
 // registers), 64-thread CTAs with 56 registers (18 CTAs per SM,
-// register_ctas 18), and 512-thread CTAs; the learned mode as 256-thread
-// (register_ctas 4) and 64-thread (18) builds; each for one seeding width
-// kLanes (lanes per h0), so that a kernel holds one copy of the seeding loop.
+// register_ctas 18), and 512-thread CTAs; the learned mode in the 64-register
+// build of up to 256 threads (a 56-register 64-thread learned build measured
+// slower: more of its registers spill around the scorer's calls); each for
+// one seeding width kLanes (lanes per h0), so that a kernel holds one copy of
+// the seeding loop.
 template <int kMaxThreads, int kMinCtas, int kMode, int kMods, int kLanes>
 __global__ void __launch_bounds__(kMaxThreads, kMinCtas) search_kernel(const SearchParams p) {
   extern __shared__ __align__(16) uint8_t dyn_smem_raw[];
@@ -1054,11 +1064,7 @@ template <int G>
 struct SearchBuilds {
   static int launch(const SearchParams& p, int grid, int block, uint32_t smem, cudaStream_t st, int reg_ctas,
                     bool compact) {
-    if (p.mlp && block <= 64 && reg_ctas == 18 && compact)
-      search_kernel<64, 18, kLearned, kCompactModules, G><<<grid, block, smem, st>>>(p);
-    else if (p.mlp && block <= 64 && reg_ctas == 18)
-      search_kernel<64, 18, kLearned, kFullModules, G><<<grid, block, smem, st>>>(p);
-    else if (p.mlp && compact)
+    if (p.mlp && compact)
       search_kernel<256, 4, kLearned, kCompactModules, G><<<grid, min(block, 256), smem, st>>>(p);
     else if (p.mlp)
       search_kernel<256, 4, kLearned, kFullModules, G><<<grid, min(block, 256), smem, st>>>(p);
@@ -1094,19 +1100,12 @@ struct SearchBuilds {
     VELO_LIMIT(search_kernel<512, 1, kPlain, kFullModules, G>);
     VELO_LIMIT(search_kernel<256, 4, kLearned, kFullModules, G>);
     VELO_LIMIT(search_kernel<256, 4, kLearned, kCompactModules, G>);
-    VELO_LIMIT(search_kernel<64, 18, kLearned, kFullModules, G>);
-    VELO_LIMIT(search_kernel<64, 18, kLearned, kCompactModules, G>);
     if (G == 32) VELO_LIMIT(search_kernel<256, 4, kDump, kFullModules, 32>);
 #undef VELO_LIMIT
     return (int)e;
   }
 
   static int occupancy(int block, uint32_t smem, int reg_ctas, int mode, bool compact, int* ctas) {
-    if (mode == kModeLearned && block <= 64 && reg_ctas == 18)
-      return compact ? (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                           ctas, search_kernel<64, 18, kLearned, kCompactModules, G>, block, smem)
-                     : (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                           ctas, search_kernel<64, 18, kLearned, kFullModules, G>, block, smem);
     if (mode == kModeLearned)
       return compact ? (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                            ctas, search_kernel<256, 4, kLearned, kCompactModules, G>, min(block, 256), smem)

@@ -25,8 +25,7 @@
 // For events in the caller's host memory (velo_sort_search on a GPU that
 // reads pageable memory coherently) gather_sort_kernel copies each event
 // into device memory in one pass and sorts it there (the sort's many small
-// dependent accesses are cheap in HBM, not across the host link), writing
-// each module it changes back into the caller's buffer as it goes.
+// dependent accesses are cheap in HBM, not across the host link).
 #include <cuda_runtime.h>
 
 #include "velo_internal.h"
@@ -90,25 +89,10 @@ struct SortStage {
   uint32_t id[kSortWarps][kRankMax];
 };
 
-// Copies hits [s0, s0 + n) of the four hit arrays of a module to the same
-// places of `mirror` (lanes of one warp).
-__device__ __forceinline__ void mirror_module(const float* x, const float* y, const float* z, const uint32_t* id,
-                                              float* mx, float* my, float* mz, uint32_t* mid, int s0, int n,
-                                              int lane) {
-  for (int i = s0 + lane; i < s0 + n; i += 32) {
-    mx[i] = x[i];
-    my[i] = y[i];
-    mz[i] = z[i];
-    mid[i] = id[i];
-  }
-}
-
 // Sorts the modules of one event in place (all threads of the CTA call it);
 // returns, in every thread, whether any byte moved.  Events whose module
-// table does not tile their hits are left alone.  With `mirror` (an event of
-// the same layout: the caller's host copy), every module the sort changes is
-// also written there.
-__device__ bool sort_event(uint8_t* event, SortStage& st, uint8_t* mirror = nullptr) {
+// table does not tile their hits are left alone.
+__device__ bool sort_event(uint8_t* event, SortStage& st) {
   int32_t* hdr = reinterpret_cast<int32_t*>(event);
   const int S = hdr[0], H = hdr[1];
   const int32_t* start = hdr + 2 + S;
@@ -117,11 +101,6 @@ __device__ bool sort_event(uint8_t* event, SortStage& st, uint8_t* mirror = null
   float* x = reinterpret_cast<float*>(id + H);
   float* y = x + H;
   float* z = y + H;
-  // the same arrays in the mirror (unused without one)
-  uint32_t* mid = mirror ? reinterpret_cast<uint32_t*>(mirror) + (2 + 3 * S) : nullptr;
-  float* mx = mirror ? reinterpret_cast<float*>(mid + H) : nullptr;
-  float* my = mirror ? mx + H : nullptr;
-  float* mz = mirror ? my + H : nullptr;
   // the module table must tile [0, H) in order before anything moves
   bool bad = threadIdx.x == 0 && S == 0 && H != 0;
   for (int m = threadIdx.x; m < S; m += blockDim.x) {
@@ -155,10 +134,6 @@ __device__ bool sort_event(uint8_t* event, SortStage& st, uint8_t* mirror = null
         }
       }
       wrote |= changed;
-      if (mirror) {
-        __syncwarp();
-        if (__shfl_sync(kFullMask, changed, 0)) mirror_module(x, y, z, id, mx, my, mz, mid, s0, n, lane);
-      }
       continue;
     }
     bool finite = true, moved = false;
@@ -199,7 +174,6 @@ __device__ bool sort_event(uint8_t* event, SortStage& st, uint8_t* mirror = null
         wrote = true;
       }
       __syncwarp();
-      if (mirror) mirror_module(x, y, z, id, mx, my, mz, mid, s0, n, lane);
       continue;
     }
     if (!__any_sync(kFullMask, moved)) continue;   // strictly increasing already
@@ -213,12 +187,6 @@ __device__ bool sort_event(uint8_t* event, SortStage& st, uint8_t* mirror = null
         y[r] = sy[i];
         z[r] = sz[i];
         id[r] = sid[i];
-        if (mirror) {   // posted writes across the host link
-          mx[r] = sx[i];
-          my[r] = sy[i];
-          mz[r] = sz[i];
-          mid[r] = sid[i];
-        }
       }
     }
     __syncwarp();   // the staging buffer is refilled for the next module
@@ -236,16 +204,19 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
 
 // Copies event e from the caller's host memory (src_base + src_off[e], a
 // 4-byte aligned buffer the device reads coherently) into the staged device
-// batch (dst + dst_off[e], 16-byte aligned) in one pass, then sorts it there
-// and writes every module the sort changed back into the caller's buffer.
-__global__ void __launch_bounds__(kSortThreads) gather_sort_kernel(uint8_t* src_base, const uint64_t* src_off,
+// batch (dst + dst_off[e], 16-byte aligned) in one pass, then sorts it
+// there; moved[e] tells whether the sort changed it.  (Writing the changed
+// modules back from here, or from a kernel of its own, costs 1.4-1.8 ms per
+// 190 MB across the host link; the search kernel's staging does it instead,
+// hidden behind the search.)
+__global__ void __launch_bounds__(kSortThreads) gather_sort_kernel(const uint8_t* src_base, const uint64_t* src_off,
                                                                    const uint64_t* sizes, uint8_t* dst,
                                                                    const uint64_t* dst_off, const uint32_t* valid,
-                                                                   int n_events) {
+                                                                   uint32_t* moved, int n_events) {
   __shared__ SortStage st;
   const int e = blockIdx.x;
   if (e >= n_events) return;
-  uint8_t* src = src_base + src_off[e];
+  const uint8_t* src = src_base + src_off[e];
   uint8_t* __restrict__ out = dst + dst_off[e];
   const uint64_t size = sizes[e];
   uint64_t done = 0;
@@ -272,7 +243,8 @@ __global__ void __launch_bounds__(kSortThreads) gather_sort_kernel(uint8_t* src_
   const uint64_t tail = done + (words << 2);
   if (threadIdx.x < size - tail) out[tail + threadIdx.x] = src[tail + threadIdx.x];
   __syncthreads();
-  if (valid[e]) sort_event(out, st, src);
+  const bool m = valid[e] ? sort_event(out, st) : false;
+  if (threadIdx.x == 0) moved[e] = m ? 1u : 0u;
 }
 
 }  // namespace
@@ -283,11 +255,11 @@ int launch_sort_modules(uint8_t* input, const uint64_t* offsets, const uint32_t*
   return (int)cudaGetLastError();
 }
 
-int launch_gather_sort(uint8_t* src_base, const uint64_t* src_off, const uint64_t* sizes, uint8_t* dst,
-                       const uint64_t* dst_off, const uint32_t* valid, int n_events, void* stream) {
+int launch_gather_sort(const uint8_t* src_base, const uint64_t* src_off, const uint64_t* sizes, uint8_t* dst,
+                       const uint64_t* dst_off, const uint32_t* valid, uint32_t* moved, int n_events, void* stream) {
   if (n_events <= 0) return 0;
   gather_sort_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(src_base, src_off, sizes, dst, dst_off,
-                                                                         valid, n_events);
+                                                                         valid, moved, n_events);
   return (int)cudaGetLastError();
 }
 
