@@ -132,13 +132,10 @@ struct velo_ctx {
   uint64_t io_capacity = 0;
   unsigned long long* io_cursor = nullptr;   // output cursor shared by pipelined parts
 
-  // velo_sort_search on a coherent host: source offsets and sizes of the
-  // events in the caller's memory
-  PinnedVec<uint64_t> h_src_offset, h_sizes;
-  DevBuf d_src_offset, d_sizes, d_moved;
-  // the batch was gathered from the caller's buffers (base): the search
-  // writes the sorted hit arrays back there
-  uint8_t* mirror_base = nullptr;
+  // the next launch x-sorts each event while staging it and writes the
+  // sorted hit arrays back into the input, read in place (velo_sort_search,
+  // velo_search_begin with sort)
+  bool sort_in_search = false;
   // streamed search in flight (velo_search_begin .. velo_search_end)
   velo_event_result* io_results = nullptr;
   bool streaming = false;
@@ -406,8 +403,7 @@ void velo_destroy(velo_ctx* c) {
                     &c->d_hit_base, &c->d_arena_off, &c->d_order, &c->d_tracklets, &c->d_rings, &c->d_weak,
                     &c->d_tracks, &c->d_out_tracks, &c->d_out_counts, &c->d_out_first,
                     &c->d_out_status, &c->d_counters, &c->d_garena, &c->d_flush, &c->d_mlp,
-                    &c->d_dump_features, &c->d_dump_ids, &c->d_fits, &c->d_src_offset, &c->d_sizes,
-                    &c->d_moved};
+                    &c->d_dump_features, &c->d_dump_ids, &c->d_fits};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -439,8 +435,7 @@ void* device_view(const void* host) {
 }
 
 velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
-                       int32_t n, bool direct, bool pageable = false, const uint64_t* dev_offsets = nullptr,
-                       uint64_t dev_total = 0);
+                       int32_t n, bool direct, bool pageable = false);
 
 }  // namespace
 
@@ -458,11 +453,9 @@ namespace {
 // Stages a batch: host checks, per-event metadata, and the events themselves
 // (copied, or with `direct` read in place when buf is mapped pinned memory;
 // with `pageable` as well, on a device with coherent access to pageable host
-// memory, read in place wherever they are).  With dev_offsets the device
-// batch is laid out at those offsets (dev_total bytes) and nothing is
-// copied: the caller fills it (launch_gather_sort).
+// memory, read in place wherever they are).
 velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
-                       int32_t n, bool direct, bool pageable, const uint64_t* dev_offsets, uint64_t dev_total) {
+                       int32_t n, bool direct, bool pageable) {
   if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
   HostTimer timer(&c->stats.host_stage_ms);
   VELO_CUDA(c, cudaSetDevice(c->device));
@@ -506,7 +499,7 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
     c->h_valid[e] = ok ? 1u : 0u;
     c->h_hits[e] = ok ? H : 0u;
     c->h_maxmod[e] = 0u;   // the arena layout depends on H only
-    c->h_offset[e] = dev_offsets ? dev_offsets[e] : offsets[e] - lo;
+    c->h_offset[e] = offsets[e] - lo;
     c->h_hit_base[e] = rows;
     rows += std::max<uint64_t>(c->h_hits[e], 1ull);
     hits += c->h_hits[e];
@@ -514,10 +507,10 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
   c->rows = rows;
   c->total_hits = hits;
   c->max_modules = max_modules;
-  c->input_bytes = dev_offsets ? dev_total : hi - lo;
+  c->input_bytes = hi - lo;
   velo_status st;
-  if (direct && hi > lo && !dev_offsets) c->io_input = static_cast<const uint8_t*>(device_view(buf + lo));
-  if (direct && pageable && hi > lo && !dev_offsets && !c->io_input && c->coherent_host) c->io_input = buf + lo;
+  if (direct && hi > lo) c->io_input = static_cast<const uint8_t*>(device_view(buf + lo));
+  if (direct && pageable && hi > lo && !c->io_input && c->coherent_host) c->io_input = buf + lo;
   if (!c->io_input && (st = ensure(c, c->d_input, c->input_bytes + 16, "input")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_offset, 8ull * n, "offsets")) != VELO_OK) return st;
   if ((st = ensure(c, c->d_ev_hits, 4ull * n, "hits")) != VELO_OK) return st;
@@ -542,7 +535,7 @@ velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets,
     VELO_CUDA(c, cudaEventRecord(c->meta_copied, c->stream));
   }
   // the events last, so that waiting for the metadata copies never waits for them
-  if (hi > lo && !c->io_input && !dev_offsets)
+  if (hi > lo && !c->io_input)
     VELO_CUDA(c, cudaMemcpyAsync(c->d_input.p, buf + lo, hi - lo, cudaMemcpyHostToDevice, c->stream));
   c->staged = true;
   return VELO_OK;
@@ -754,11 +747,7 @@ velo_status enqueue_kernel(velo_ctx* c, const velo_options& o, uint32_t smem, in
   p.out_status = P<uint32_t>(c->d_out_status);
   p.out_cursor = c->io_cursor ? c->io_cursor : P<unsigned long long>(c->d_counters);
   p.results = c->io_results;
-  if (c->mirror_base) {
-    p.mirror_base = c->mirror_base;
-    p.mirror_offset = P<uint64_t>(c->d_src_offset);
-    p.mirror_moved = P<uint32_t>(c->d_moved);
-  }
+  p.sort_events = c->sort_in_search && c->io_input ? 1 : 0;
   p.work_counter = reinterpret_cast<int32_t*>(P<uint8_t>(c->d_counters) + 32);
   if (o.learned) {
     p.mlp = P<float>(c->d_mlp);
@@ -1239,8 +1228,11 @@ velo_status search_in_place(velo_ctx* c, const uint8_t* base, const uint64_t* of
   c->io_cursor = nullptr;
   velo_status st = stage_impl(c, base, offs, sizes, n, true, true);
   *read_in_place = c->io_input != nullptr;
-  if (st == VELO_OK && sort && !*read_in_place) st = VELO_ERR_INVALID_ARGUMENT;   // never: base is readable
-  if (st == VELO_OK && sort) st = velo_sort_staged(c);
+  if (st == VELO_OK && sort && !*read_in_place && n > 0) {   // never: base is device-readable
+    c->err = "events to sort are not readable in place";
+    st = VELO_ERR_INVALID_ARGUMENT;
+  }
+  c->sort_in_search = sort;   // the search kernel sorts while staging, and writes back
   if (st == VELO_OK) st = velo_run(c, &o);
   if (st == VELO_OK) st = velo_fetch(c, tracks_out, capacity, counts, first, status);
   uint64_t bytes = 0;
@@ -1249,6 +1241,7 @@ velo_status search_in_place(velo_ctx* c, const uint8_t* base, const uint64_t* of
   c->io_input = nullptr;
   c->io_tracks = nullptr;
   c->io_capacity = 0;
+  c->sort_in_search = false;
   c->staged = false;   // the batch pointed into the caller's buffers
   c->ran = false;
   c->generation++;
@@ -1258,46 +1251,6 @@ velo_status search_in_place(velo_ctx* c, const uint8_t* base, const uint64_t* of
       c->err = "event " + std::to_string(e) + " failed validation";
       return VELO_ERR_INVALID_EVENT;
     }
-  return VELO_OK;
-}
-
-// Device-side layout of a gathered batch: packed, 16-byte aligned.
-uint64_t packed_offsets(const uint64_t* sizes, int32_t n, std::vector<uint64_t>& dev_offs) {
-  dev_offs.resize(n);
-  uint64_t total = 0;
-  for (int32_t e = 0; e < n; ++e) {
-    dev_offs[e] = total;
-    total += (sizes[e] + 15) & ~15ull;
-  }
-  return total;
-}
-
-// After stage_impl with dev_offsets: one kernel copies every event from the
-// caller's buffer (base + src_offs[e]) into device memory and sorts it
-// there; the search then runs on the device copy and, while it stages each
-// event, writes the hit arrays the sort changed back into the caller's
-// buffer (mirror_base), hidden behind the search.
-velo_status enqueue_gather_sort(velo_ctx* c, uint8_t* base, const uint64_t* src_offs, const uint64_t* sizes,
-                                int32_t n) {
-  if (n <= 0) return VELO_OK;
-  // the previous batch's copies out of these pinned arrays are done
-  // (stage_impl waited for meta_copied, recorded after them)
-  if (!c->h_src_offset.assign(n, 0) || !c->h_sizes.assign(n, 0)) return VELO_ERR_OUT_OF_MEMORY;
-  std::memcpy(c->h_src_offset.data(), src_offs, 8ull * n);
-  std::memcpy(c->h_sizes.data(), sizes, 8ull * n);
-  velo_status st;
-  if ((st = ensure(c, c->d_src_offset, 8ull * n, "source offsets")) != VELO_OK) return st;
-  if ((st = ensure(c, c->d_sizes, 8ull * n, "sizes")) != VELO_OK) return st;
-  if ((st = ensure(c, c->d_moved, 4ull * n, "moved")) != VELO_OK) return st;
-  VELO_CUDA(c, cudaMemcpyAsync(c->d_src_offset.p, c->h_src_offset.data(), 8ull * n, cudaMemcpyHostToDevice,
-                               c->stream));
-  VELO_CUDA(c, cudaMemcpyAsync(c->d_sizes.p, c->h_sizes.data(), 8ull * n, cudaMemcpyHostToDevice, c->stream));
-  VELO_CUDA(c, cudaEventRecord(c->meta_copied, c->stream));
-  const int e = velo::launch_gather_sort(base, P<uint64_t>(c->d_src_offset), P<uint64_t>(c->d_sizes),
-                                         P<uint8_t>(c->d_input), P<uint64_t>(c->d_ev_offset),
-                                         P<uint32_t>(c->d_ev_valid), P<uint32_t>(c->d_moved), n, c->stream);
-  if (e != 0) return cuda_fail(c, (cudaError_t)e, "gather-sort kernel launch");
-  c->mirror_base = base;
   return VELO_OK;
 }
 
@@ -1315,39 +1268,12 @@ velo_status end_in_place(velo_ctx* c, velo_status r) {
   c->io_tracks = nullptr;
   c->io_capacity = 0;
   c->io_results = nullptr;
-  c->mirror_base = nullptr;
+  c->sort_in_search = false;
   c->streaming = false;
   c->staged = false;
   c->ran = false;
   c->generation++;
   return r;
-}
-
-// velo_sort_search on a device that reads the caller's host memory
-// coherently (enqueue_gather_sort), searched on the device copy.
-velo_status sort_search_gathered(velo_ctx* c, uint8_t* base, const uint64_t* src_offs, const uint64_t* sizes,
-                                 int32_t n, velo_options o, velo_track* tracks_out, uint64_t capacity,
-                                 uint32_t* counts, uint64_t* first, uint32_t* status) {
-  o.use_graph = 0;
-  std::vector<uint64_t> dev_offs;
-  const uint64_t total = packed_offsets(sizes, n, dev_offs);
-  c->io_tracks = tracks_in_place(c, tracks_out, capacity);
-  c->io_capacity = c->io_tracks ? capacity : 0;
-  c->io_cursor = nullptr;
-  velo_status st = stage_impl(c, base, src_offs, sizes, n, false, false, dev_offs.data(), total);
-  if (st == VELO_OK) st = enqueue_gather_sort(c, base, src_offs, sizes, n);
-  if (st != VELO_OK) return end_in_place(c, st);
-  st = velo_run(c, &o);
-  // velo_fetch synchronises the stream: the sort's writes into the caller's
-  // buffers are complete too
-  if (st == VELO_OK) st = velo_fetch(c, tracks_out, capacity, counts, first, status);
-  if (st != VELO_OK) return end_in_place(c, st);
-  for (int32_t e = 0; e < n; ++e)
-    if (c->h_status[e] & VELO_EVENT_INVALID) {
-      c->err = "event " + std::to_string(e) + " failed validation";
-      return end_in_place(c, VELO_ERR_INVALID_EVENT);
-    }
-  return end_in_place(c, VELO_OK);
 }
 
 }  // namespace
@@ -1400,10 +1326,13 @@ velo_status velo_sort_search(velo_ctx* c, uint8_t* const* events, const uint64_t
   std::vector<uint64_t> offs;
   bool in_place = false;
   if (c->coherent_host && o.host_direct) {
+    // sorted (while the search kernel stages each event) and searched where
+    // the caller's buffers lie
     const uint8_t* base = nullptr;
     offsets_in_place(events, sizes, n, &base, offs);
-    return sort_search_gathered(c, const_cast<uint8_t*>(base), offs.data(), sizes, n, o, tracks_out, capacity,
-                                counts, first, status);
+    st = search_in_place(c, base, offs.data(), sizes, n, o, true, tracks_out, capacity, counts, first, status,
+                         &in_place);
+    if (in_place || n == 0 || st != VELO_OK) return st;
   }
   // packed into pinned memory, sorted and searched there, the sorted bytes
   // copied back into the caller's buffers
@@ -1447,27 +1376,26 @@ velo_status velo_search_begin(velo_ctx* c, uint8_t* const* events, const uint64_
     c->err = "batch larger than the device budget: call with fewer events";
     return VELO_ERR_OUT_OF_MEMORY;
   }
-  std::vector<uint64_t> offs, dev_offs;
+  std::vector<uint64_t> offs;
   const uint8_t* base = nullptr;
   offsets_in_place(events, sizes, n, &base, offs);
   std::memset(results, 0, sizeof(velo_event_result) * (size_t)n);
   c->io_tracks = tracks_in_place(c, tracks_out, capacity);
   c->io_capacity = capacity;
   c->io_cursor = nullptr;
-  if (sort) {
-    const uint64_t total = packed_offsets(sizes, n, dev_offs);
-    st = stage_impl(c, base, offs.data(), sizes, n, false, false, dev_offs.data(), total);
-  } else {
-    st = stage_impl(c, base, offs.data(), sizes, n, true, true);
-  }
+  st = stage_impl(c, base, offs.data(), sizes, n, true, true);   // read in place
   if (st == VELO_OK && c->rows > capacity) {
     c->err = "track buffer holds " + std::to_string(capacity) + " tracks, velo_track_capacity is " +
              std::to_string(c->rows);
     st = VELO_ERR_INVALID_ARGUMENT;
   }
-  if (st == VELO_OK && sort) st = enqueue_gather_sort(c, const_cast<uint8_t*>(base), offs.data(), sizes, n);
+  if (st == VELO_OK && n > 0 && !c->io_input) {
+    c->err = "events not readable in place";
+    st = VELO_ERR_INVALID_ARGUMENT;
+  }
   if (st != VELO_OK) return end_in_place(c, st);
   c->io_results = results;
+  c->sort_in_search = sort != 0;   // the search kernel sorts while staging, and writes back
   st = velo_run(c, &o);
   if (st != VELO_OK) {
     cudaStreamSynchronize(c->stream);

@@ -123,13 +123,11 @@ struct SearchParams {
   uint32_t* out_status;
   unsigned long long* out_cursor; // running total of compacted tracks
   velo_event_result* results;     // streaming (velo_search_begin): per-event records in host memory, or null
-  // velo_sort_search / velo_search_begin with sort: the caller's buffers
-  // (event e at mirror_base + mirror_offset[e]) that receive the sorted hit
-  // arrays of the events whose sort moved something (mirror_moved[e]); null
-  // mirror_base = nothing to write back
-  uint8_t* mirror_base;
-  const uint64_t* mirror_offset;
-  const uint32_t* mirror_moved;
+  // velo_sort_search / velo_search_begin with sort: each event's modules are
+  // x-sorted (the reference's permutation) while the event is staged, and
+  // the sorted hit arrays are written back into the input, which is then
+  // the caller's buffer read in place
+  int32_t sort_events;
   int32_t* work_counter;          // persistent mode queue head
   // training data: features and {event, h0, h1} of sampled doublets
   float* dump_features;
@@ -163,12 +161,6 @@ int launch_fit_tracks(const uint8_t* input, const uint64_t* ev_offset, const uin
                       velo_track_fit* fits, void* stream);
 // Sorts each module's hits by x in place on staged events (velo_sort.cu).
 int launch_sort_modules(uint8_t* input, const uint64_t* offsets, const uint32_t* valid, int n_events, void* stream);
-// Copies each event from host memory the device reads coherently
-// (src_base + src_off[e]) into the staged batch (dst + dst_off[e]) and sorts
-// it there; moved[e] = 1 where the sort changed the event (velo_sort.cu).
-// The search kernel writes those events' hit arrays back (mirror_*).
-int launch_gather_sort(const uint8_t* src_base, const uint64_t* src_off, const uint64_t* sizes, uint8_t* dst,
-                       const uint64_t* dst_off, const uint32_t* valid, uint32_t* moved, int n_events, void* stream);
 // kernel modes (velo_kernels.cu): plain, plain + training-data dump, learned
 constexpr int kModePlain = 0, kModeDump = 1, kModeLearned = 2;
 

@@ -48,6 +48,7 @@
 
 #include "velo_internal.h"
 #include "velo_mlp_warp.cuh"
+#include "velo_partition.cuh"
 
 namespace velo {
 
@@ -757,6 +758,103 @@ static __device__ unsigned long long g_phase_cycles[8];   // one per translation
 #define VELO_PHASE_END() do {} while (0)
 #endif
 
+// Hits of a module that one warp sorts by rank in registers (4 per lane).
+constexpr int kArenaRankMax = 128;
+
+// The reference's per-module x-sort (preorder_by_x, Tools.cpp:46-66) of the
+// event staged in the arena, hit IDs alongside in `ids`; one warp per
+// module.  Where a module's x values are distinct the reference's quicksort
+// reaches the one ascending order there is, so each hit goes to its rank;
+// a module with equal x values, or more than kArenaRankMax hits not already
+// in strictly increasing order, replays the reference's partition steps in
+// one thread (quicksort4).  x is finite here (the staging checked it).
+// Returns, in every thread, whether any hit moved.
+template <class Shared>
+__device__ bool sort_arena(const EventView& ev, const Shared& s, int S, uint32_t* ids) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  float* x = ev.xs();
+  float* y = ev.ys();
+  float* z = ev.zs();
+  bool moved = false;
+  for (int m = warp; m < S; m += nwarps) {   // warp-uniform
+    const int s0 = s.start[m], n = s.num[m];
+    if (n < 2) continue;
+    if (n > kArenaRankMax) {
+      bool changed = false;
+      if (lane == 0) {
+        bool increasing = true;
+        for (int i = s0 + 1; i < s0 + n && increasing; ++i) increasing = x[i - 1] < x[i];
+        if (!increasing) {
+          quicksort4(x, y, z, ids, s0, s0 + n - 1);
+          changed = true;
+        }
+      }
+      moved |= __shfl_sync(kFull, changed, 0);
+      __syncwarp();
+      continue;
+    }
+    float xr[4];
+    int rk[4], eq[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = lane + 32 * k;
+      xr[k] = i < n ? x[s0 + i] : 0.f;
+      rk[k] = 0;
+      eq[k] = 0;
+    }
+    for (int j = 0; j < n; ++j) {   // the same address in every lane
+      const float xj = x[s0 + j];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        rk[k] += xj < xr[k];
+        eq[k] += xj == xr[k];
+      }
+    }
+    bool tie = false, mv = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = lane + 32 * k;
+      if (i < n) {
+        tie |= eq[k] > 1;
+        mv |= rk[k] != i;
+      }
+    }
+    if (__any_sync(kFull, tie)) {   // equal x values: the reference's partition steps decide
+      if (lane == 0) quicksort4(x, y, z, ids, s0, s0 + n - 1);
+      moved = true;
+      __syncwarp();
+      continue;
+    }
+    if (!__any_sync(kFull, mv)) continue;   // strictly increasing already
+    moved = true;
+    float yr[4], zr[4];
+    uint32_t ir[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = lane + 32 * k;
+      if (i < n) {
+        yr[k] = y[s0 + i];
+        zr[k] = z[s0 + i];
+        ir[k] = ids[s0 + i];
+      }
+    }
+    __syncwarp();   // every lane has read its hits before any is overwritten
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = lane + 32 * k;
+      if (i < n) {
+        const int r = s0 + rk[k];
+        x[r] = xr[k];
+        y[r] = yr[k];
+        z[r] = zr[k];
+        ids[r] = ir[k];
+      }
+    }
+    __syncwarp();
+  }
+  return __syncthreads_or(moved) != 0;
+}
+
 // Streaming results (velo_search_begin): thread 0 writes the event's record,
 // its ready flag last, after a system-scope fence; the caller has fenced the
 // CTA's track writes before.
@@ -834,14 +932,10 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     s.num[m] = nm;
     s.sz[m] = gZ[m];
   }
-  if (p.mirror_base && p.mirror_moved[e]) {
-    // the sorted hit arrays (IDs, x, y, z) back into the caller's buffer,
-    // which this batch was gathered from: posted writes across the host
-    // link, overlapped with the search of this and the other resident events
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(gnum + S);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(p.mirror_base + p.mirror_offset[e]) + (2 + 3 * S);
-    for (int w = tid; w < 4 * H; w += nt) dst[w] = src[w];
-  }
+  // with sort_events the IDs are staged too, in the window area (written
+  // only after the sort)
+  const uint32_t* gid = reinterpret_cast<const uint32_t*>(gnum + S);
+  uint32_t* ids = reinterpret_cast<uint32_t*>(ev.wins());
   for (int i = tid; i < H; i += nt) {
     const float xv = gx[i], yv = gy[i], zv = gz[i];
     bad |= !(isfinite(xv) && isfinite(yv) && isfinite(zv));
@@ -849,6 +943,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     ev.ys()[i] = yv;
     ev.zs()[i] = zv;
     ev.useds()[i] = 0;
+    if (p.sort_events) ids[i] = gid[i];
   }
   if (tid == 0) {
     s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
@@ -863,6 +958,22 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       if (p.results) publish_result(p, e, 0ull, 0u, VELO_EVENT_INVALID);
     }
     return;
+  }
+  if (p.sort_events && sort_arena(ev, s, S, ids)) {
+    // the sorted hit arrays (IDs, x, y, z) back into the input, the
+    // caller's buffer read in place: posted writes across the host link,
+    // overlapped with the search of the other resident events
+    uint32_t* wid = const_cast<uint32_t*>(gid);
+    float* wx = reinterpret_cast<float*>(wid + H);
+    float* wy = wx + H;
+    float* wz = wy + H;
+    for (int i = tid; i < H; i += nt) {
+      wid[i] = ids[i];
+      wx[i] = ev.xs()[i];
+      wy[i] = ev.ys()[i];
+      wz[i] = ev.zs()[i];
+    }
+    __syncthreads();   // the window area is written next
   }
   VELO_PHASE(0);
 

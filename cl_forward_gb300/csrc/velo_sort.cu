@@ -22,13 +22,12 @@
 //  * a module with a non-finite x is left alone: the reference's sort does
 //    not return on a NaN, and the search marks such an event invalid.
 //
-// For events in the caller's host memory (velo_sort_search on a GPU that
-// reads pageable memory coherently) gather_sort_kernel copies each event
-// into device memory in one pass and sorts it there (the sort's many small
-// dependent accesses are cheap in HBM, not across the host link).
+// velo_sort_search sorts inside the search kernel instead, while it stages
+// each event (velo_search_kernel.cuh: sort_arena), with the same rules.
 #include <cuda_runtime.h>
 
 #include "velo_internal.h"
+#include "velo_partition.cuh"
 
 namespace velo {
 namespace {
@@ -37,50 +36,6 @@ constexpr unsigned kFullMask = 0xffffffffu;
 constexpr int kSortThreads = 128;              // 4 warps per event
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kRankMax = 256;                  // hits a warp stages (16 B each)
-
-__device__ __forceinline__ void swap4(float* a, float* b, float* c, uint32_t* d, int i, int j) {
-  float t = a[i]; a[i] = a[j]; a[j] = t;
-  t = b[i]; b[i] = b[j]; b[j] = t;
-  t = c[i]; c[i] = c[j]; c[j] = t;
-  const uint32_t u = d[i]; d[i] = d[j]; d[j] = u;
-}
-
-__device__ int partition4(float* a, float* b, float* c, uint32_t* d, int lo, int hi) {
-  const float pivot = a[lo];
-  int l = lo, r = hi;
-  while (l < r) {
-    while (a[r] > pivot) r--;   // stops at lo at the latest: a[lo] == pivot
-    while (l < r && a[l] <= pivot) l++;
-    if (l < r) swap4(a, b, c, d, l, r);
-  }
-  swap4(a, b, c, d, r, lo);
-  return r;
-}
-
-constexpr int kStack = 64;   // >= 2 * log2(VELO_MAX_MODULE_HITS + 1) + 2
-
-// The reference's partition steps over [lo, hi] (one thread).
-__device__ void quicksort4(float* x, float* y, float* z, uint32_t* id, int lo0, int hi0) {
-  int lo_s[kStack], hi_s[kStack];
-  int sp = 0;
-  lo_s[sp] = lo0;
-  hi_s[sp] = hi0;
-  sp++;
-  while (sp > 0 && sp <= kStack - 2) {
-    --sp;
-    const int lo = lo_s[sp], hi = hi_s[sp];
-    if (lo >= hi) continue;
-    const int p = partition4(x, y, z, id, lo, hi);
-    // push the larger side first so the smaller one is processed next
-    if (p - lo > hi - p) {
-      lo_s[sp] = lo; hi_s[sp] = p - 1; sp++;
-      lo_s[sp] = p + 1; hi_s[sp] = hi; sp++;
-    } else {
-      lo_s[sp] = p + 1; hi_s[sp] = hi; sp++;
-      lo_s[sp] = lo; hi_s[sp] = p - 1; sp++;
-    }
-  }
-}
 
 struct SortStage {
   float x[kSortWarps][kRankMax];
@@ -202,64 +157,11 @@ __global__ void __launch_bounds__(kSortThreads) sort_modules_kernel(uint8_t* inp
   sort_event(input + offsets[e], st);
 }
 
-// Copies event e from the caller's host memory (src_base + src_off[e], a
-// 4-byte aligned buffer the device reads coherently) into the staged device
-// batch (dst + dst_off[e], 16-byte aligned) in one pass, then sorts it
-// there; moved[e] tells whether the sort changed it.  (Writing the changed
-// modules back from here, or from a kernel of its own, costs 1.4-1.8 ms per
-// 190 MB across the host link; the search kernel's staging does it instead,
-// hidden behind the search.)
-__global__ void __launch_bounds__(kSortThreads) gather_sort_kernel(const uint8_t* src_base, const uint64_t* src_off,
-                                                                   const uint64_t* sizes, uint8_t* dst,
-                                                                   const uint64_t* dst_off, const uint32_t* valid,
-                                                                   uint32_t* moved, int n_events) {
-  __shared__ SortStage st;
-  const int e = blockIdx.x;
-  if (e >= n_events) return;
-  const uint8_t* src = src_base + src_off[e];
-  uint8_t* __restrict__ out = dst + dst_off[e];
-  const uint64_t size = sizes[e];
-  uint64_t done = 0;
-  if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {   // 16-byte words, four in flight per thread
-    const uint64_t n16 = size >> 4;
-    const uint4* __restrict__ s16 = reinterpret_cast<const uint4*>(src);
-    uint4* __restrict__ d16 = reinterpret_cast<uint4*>(out);
-    uint64_t i = threadIdx.x;
-    for (; i + 3 * kSortThreads < n16; i += 4 * kSortThreads) {
-      const uint4 a = s16[i], b = s16[i + kSortThreads], c = s16[i + 2 * kSortThreads],
-                  d = s16[i + 3 * kSortThreads];
-      d16[i] = a;
-      d16[i + kSortThreads] = b;
-      d16[i + 2 * kSortThreads] = c;
-      d16[i + 3 * kSortThreads] = d;
-    }
-    for (; i < n16; i += kSortThreads) d16[i] = s16[i];
-    done = n16 << 4;
-  }
-  const uint64_t words = (size - done) >> 2;
-  const uint32_t* __restrict__ s4 = reinterpret_cast<const uint32_t*>(src + done);
-  uint32_t* __restrict__ d4 = reinterpret_cast<uint32_t*>(out + done);
-  for (uint64_t i = threadIdx.x; i < words; i += kSortThreads) d4[i] = s4[i];
-  const uint64_t tail = done + (words << 2);
-  if (threadIdx.x < size - tail) out[tail + threadIdx.x] = src[tail + threadIdx.x];
-  __syncthreads();
-  const bool m = valid[e] ? sort_event(out, st) : false;
-  if (threadIdx.x == 0) moved[e] = m ? 1u : 0u;
-}
-
 }  // namespace
 
 int launch_sort_modules(uint8_t* input, const uint64_t* offsets, const uint32_t* valid, int n_events, void* stream) {
   if (n_events <= 0) return 0;
   sort_modules_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(input, offsets, valid, n_events);
-  return (int)cudaGetLastError();
-}
-
-int launch_gather_sort(const uint8_t* src_base, const uint64_t* src_off, const uint64_t* sizes, uint8_t* dst,
-                       const uint64_t* dst_off, const uint32_t* valid, uint32_t* moved, int n_events, void* stream) {
-  if (n_events <= 0) return 0;
-  gather_sort_kernel<<<n_events, kSortThreads, 0, (cudaStream_t)stream>>>(src_base, src_off, sizes, dst, dst_off,
-                                                                         valid, moved, n_events);
   return (int)cudaGetLastError();
 }
 

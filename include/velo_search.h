@@ -106,7 +106,8 @@ typedef struct velo_options {
                                  buffers are copied as usual.  velo_search and
                                  velo_sort_search: the same, and on a device with coherent
                                  access to pageable host memory (NVLink-C2C) the events are
-                                 read (and sorted) in the caller's own buffers, unpacked.
+                                 read from the caller's own buffers, unpacked (and with
+                                 velo_sort_search sorted in device memory and written back).
                                  Results are identical; the context holds no staged batch
                                  afterwards.  0 = off */
   int32_t device_budget_mb;   /* velo_search / velo_search_packed: device memory one call may
@@ -182,9 +183,11 @@ velo_status velo_search(velo_ctx* ctx, const uint8_t* const* events, const uint6
  * aligned.  With opts->host_direct on a device that reads and writes
  * pageable host memory coherently (cudaDevAttrPageableMemoryAccess and
  * ...UsesHostPageTables, as a Grace-coupled GPU over NVLink-C2C does), the
- * device sorts and reads the events where they lie, and writes the tracks
- * into tracks_out in place; otherwise the events are packed into pinned
- * memory, sorted and searched there, and the sorted bytes are copied back.
+ * device copies each event from the caller's buffer into its own memory,
+ * sorts and searches it there, writes the sorted hit arrays back into the
+ * caller's buffer and the tracks into tracks_out in place; otherwise the
+ * events are packed into pinned memory, sorted and searched there, and the
+ * sorted bytes are copied back.
  * A batch larger than the device budget is refused (VELO_ERR_OUT_OF_MEMORY):
  * call with fewer events.  Events that fail validation are left unsorted.
  */
