@@ -275,7 +275,7 @@ void sort_range(float* a, float* b, float* c, uint32_t* d, int lo, int hi) {
 }
 
 // Seeding lanes per h0 when the caller leaves the choice to the library.
-constexpr int32_t kDefaultSeedLanes = 16;
+constexpr int32_t kDefaultSeedLanes = 8;
 
 uint32_t resolve_threads(int32_t t) {
   if (t == 32 || t == 64 || t == 128 || t == 256 || t == 512) return (uint32_t)t;

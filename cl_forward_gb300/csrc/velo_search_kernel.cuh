@@ -78,6 +78,7 @@ struct SharedT {
   uint32_t considered, kept;   // learned seeding: doublets scored / kept
   unsigned long long out_first;
   int32_t next_event;
+  int32_t seed_next[2];  // G < 32: next unclaimed h0 of the module being seeded, by ring parity
 };
 
 struct EventView {
@@ -527,15 +528,24 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, const
   uint32_t zk0 = 0x7fc00001u, zk1 = 0x7fc00001u;
   float dz_inv_cached = 0.f;
 
-  for (int ib = warp * kGroups; ib < n0; ib += nwarps * kGroups) {   // warp-uniform
+  // G = 32: h0s dealt to the warps in turn; G < 32: each warp claims its
+  // next 32 / G h0s from a shared counter (one atomic per warp and claim),
+  // which evens out the warps' work before the barrier that ends seeding
+  int ib = G == 32 ? warp : 0;
+  if constexpr (G < 32) {
+    if (lane == 0) ib = atomicAdd(&s.seed_next[nb ^ 1], kGroups);   // seed_next[b] of the module loop
+    ib = __shfl_sync(kFull, ib, 0);
+  }
+  for (; ib < n0;) {   // warp-uniform
+    do {   // one claim of h0s; `break` moves on to the next claim
     int h0, n1, c_end;
     uint32_t f1;
     if constexpr (G == 32) {
       h0 = st0 + ib;
-      if (ev.useds()[h0]) continue;                     // warp-uniform
+      if (ev.useds()[h0]) break;                        // warp-uniform
       const uint32_t w0 = ev.wins()[h0].x;
       f1 = w0 & 0xffffu;
-      if (f1 == kNone16) continue;
+      if (f1 == kNone16) break;
       n1 = (int)(w0 >> 16) - (int)f1;                   // > 0 when a first hit was found
       c_end = n1;
     } else {
@@ -548,7 +558,7 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, const
         if (f1 != kNone16) n1 = (int)(w0 >> 16) - (int)f1;
       }
       const int chunks = (int)__reduce_max_sync(kFull, (uint32_t)((n1 + G - 1) >> kShift));
-      if (chunks == 0) continue;                        // warp-uniform
+      if (chunks == 0) break;                           // warp-uniform
       c_end = chunks << kShift;
     }
     float h0x = 0.f, h0y = 0.f, h0z = 0.f;
@@ -728,6 +738,13 @@ __device__ void seed_module(const EventView& ev, Shared& s, int f, int nb, const
         if (ri < ev.ring_cap)
           ring_buf(ev, nb)[ev.ring_cap - 1u - ri] = make_uint4(kTrackletFlag | tp, (uint32_t)h0, h1, h2);
       }
+    }
+    } while (0);
+    if constexpr (G == 32) {
+      ib += nwarps;
+    } else {
+      if (lane == 0) ib = atomicAdd(&s.seed_next[nb ^ 1], kGroups);
+      ib = __shfl_sync(kFull, ib, 0);
     }
   }
   if (degenerate) atomicOr(&s.status, VELO_EVENT_DEGENERATE);
@@ -949,6 +966,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
     s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
     s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
     s.considered = 0; s.kept = 0;
+    s.seed_next[0] = 0; s.seed_next[1] = 0;
   }
   if (__syncthreads_or(bad)) {   // a bad module table, or a non-finite coordinate
     if (tid == 0) {
@@ -1033,6 +1051,7 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       if (tid == 0) {
         s.ring_lo[0] = 0; s.ring_lo[1] = 0; s.ring_hi[0] = 0; s.ring_hi[1] = 0;
         s.ntracks = 0; s.ntracklets = 0; s.nweak = 0; s.status = 0;
+        s.seed_next[0] = 0; s.seed_next[1] = 0;
       }
       __syncthreads();
     }
@@ -1048,6 +1067,10 @@ __device__ void process_event(const SearchParams& p, int e, Shared& s, uint8_t* 
       VELO_PHASE(3);
       if (tid == 0) {
         if (ncur + s.ring_lo[b ^ 1] > VELO_TTF_MODULO) s.status |= VELO_EVENT_RING_OVERFLOW;
+        // this iteration's seeding claims h0s from seed_next[b]; the next
+        // one (parity b ^ 1) from seed_next[b ^ 1], last used before the
+        // barrier that closed the previous iteration
+        s.seed_next[b ^ 1] = 0;
         s.ring_lo[b] = 0;   // ring[b] is refilled two iterations on
         s.ring_hi[b] = 0;
       }
