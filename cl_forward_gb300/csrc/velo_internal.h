@@ -1,5 +1,6 @@
 // velo_internal.h -- definitions shared by the host orchestration
-// (velo_capi.cpp) and the sm_103a kernels (velo_kernels.cu).
+// (velo_capi.cpp) and the sm_103a kernels (velo_search_kernel.cuh, launched
+// from velo_kernels.cu).
 #pragma once
 
 #include <stdint.h>
@@ -161,7 +162,7 @@ int launch_fit_tracks(const uint8_t* input, const uint64_t* ev_offset, const uin
                       velo_track_fit* fits, void* stream);
 // Sorts each module's hits by x in place on staged events (velo_sort.cu).
 int launch_sort_modules(uint8_t* input, const uint64_t* offsets, const uint32_t* valid, int n_events, void* stream);
-// kernel modes (velo_kernels.cu): plain, plain + training-data dump, learned
+// kernel modes (velo_search_kernel.cuh): plain, plain + training-data dump, learned
 constexpr int kModePlain = 0, kModeDump = 1, kModeLearned = 2;
 
 }  // namespace velo
