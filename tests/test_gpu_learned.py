@@ -103,6 +103,30 @@ def test_learned_with_nothing_pruned_equals_plain(gpu_ctx, oracle_lib):
         assert len(got[e]) == 0
 
 
+@pytest.mark.parametrize("lanes", [8, 32])
+def test_learned_gate_above_every_window_scores_nothing(gpu_ctx, oracle_lib, lanes):
+    """learned_min_window: doublets whose exact h2 window holds fewer hits
+    than the gate are searched exactly, unscored.  With a network that would
+    prune everything (keep threshold above any logit) and a gate above every
+    window, nothing is scored, so the tracks are the plain method's and no
+    event falls back (the keep-rate guard counts scored doublets only); at a
+    gate of 0 the same network prunes every doublet and every event falls
+    back to the plain search."""
+    from cl_forward_gb300 import generator, learned, native
+    blobs = [oracle_lib.sort_by_x(b) for b in generator.generate(range(100200, 100230))[0]]
+    want, _ = oracle_lib.search(blobs, 4)
+    gpu_ctx.set_mlp(learned.init_weights(0), keep_threshold=1e30, window_margin=0.0, min_keep_rate=0.5)
+    got, status = gpu_ctx.search(blobs, native.default_options(learned=1, learned_min_window=1 << 20,
+                                                               seed_lanes=lanes))
+    assert not np.any(status & native.EVENT_LEARNED_FALLBACK)
+    assert [index_lists(g) for g in got] == [index_lists(w) for w in want]
+    got, status = gpu_ctx.search(blobs, native.default_options(learned=1, learned_min_window=0, seed_lanes=lanes))
+    assert np.all(status & native.EVENT_LEARNED_FALLBACK)
+    assert [index_lists(g) for g in got] == [index_lists(w) for w in want]
+    with pytest.raises(native.VeloError):
+        gpu_ctx.search(blobs, native.default_options(learned=1, learned_min_window=-1))
+
+
 def test_trained_network_gains_over_untrained(gpu_ctx, oracle_lib):
     """Same recall target on held-out doublets: the trained scorer prunes much
     more, and the pruned search stays within 0.5 % efficiency and 0.2 % ghost
