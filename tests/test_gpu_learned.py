@@ -154,3 +154,38 @@ def test_trained_network_gains_over_untrained(gpu_ctx, oracle_lib):
     print(f"kept {kept_trained:.3f} (untrained {kept_random:.3f}); plain {p['events_per_s']:.0f} ev/s "
           f"eff {p['efficiency']:.4f} ghost {p['ghost_rate']:.4f}; learned {l['events_per_s']:.0f} ev/s "
           f"eff {l['efficiency']:.4f} ghost {l['ghost_rate']:.4f} fallback {l['fallback']}")
+
+
+def test_learned_through_streamed_and_sorting_paths(gpu_ctx, oracle_lib):
+    """The learned kernel shares the staging, the in-kernel sort and the
+    streamed records with the plain one: velo_search_begin (with and without
+    the sort) and velo_sort_search give the tracks of the synchronous learned
+    search of the pre-sorted events, event by event."""
+    import time
+    from cl_forward_gb300 import generator, native
+    wz = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "..", "cl_forward_gb300",
+                                             "weights", "doublet_mlp.npz"))
+    gpu_ctx.set_mlp(wz["weights"], float(wz["keep_threshold"]), float(wz["window_margin"]),
+                    float(wz["min_keep_rate"]), int(wz["max_event_hits"]))
+    raw = generator.generate(range(100300, 100360))[0]
+    srt = [oracle_lib.sort_by_x(b) for b in raw]
+    o = native.default_options(learned=1, host_direct=1)
+    want, wst = gpu_ctx.search(srt, o)
+    for sort, src in ((0, srt), (1, raw)):
+        bufs = [bytearray(b) for b in src]
+        results, tracks, keep = gpu_ctx.search_begin(bufs, sort=bool(sort), options=o)
+        t0 = time.perf_counter()
+        while not results["ready"].all():
+            assert time.perf_counter() - t0 < 60
+            time.sleep(0.0005)
+        counts, first, status = gpu_ctx.search_end(len(bufs))
+        assert [bytes(b) for b in bufs] == srt
+        assert np.array_equal(status, wst)
+        for e in range(len(src)):
+            got = tracks[int(first[e]):int(first[e]) + int(counts[e])]
+            assert index_lists(got) == index_lists(want[e]), (sort, e)
+        del keep
+    bufs = [bytearray(b) for b in raw]
+    got, status = gpu_ctx.sort_search(bufs, o)
+    assert [bytes(b) for b in bufs] == srt and np.array_equal(status, wst)
+    assert [index_lists(g) for g in got] == [index_lists(w) for w in want]
