@@ -161,10 +161,10 @@ def test_learned_through_streamed_and_sorting_paths(gpu_ctx, oracle_lib):
     streamed records with the plain one: velo_search_begin (with and without
     the sort) and velo_sort_search give the tracks of the synchronous learned
     search of the pre-sorted events, event by event."""
+    import os
     import time
     from cl_forward_gb300 import generator, native
-    wz = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "..", "cl_forward_gb300",
-                                             "weights", "doublet_mlp.npz"))
+    wz = np.load(os.path.join(os.path.dirname(__file__), "..", "cl_forward_gb300", "weights", "doublet_mlp.npz"))
     gpu_ctx.set_mlp(wz["weights"], float(wz["keep_threshold"]), float(wz["window_margin"]),
                     float(wz["min_keep_rate"]), int(wz["max_event_hits"]))
     raw = generator.generate(range(100300, 100360))[0]
