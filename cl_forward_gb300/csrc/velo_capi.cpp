@@ -172,6 +172,15 @@ velo_status cuda_fail(velo_ctx* c, cudaError_t e, const char* what) {
     if (_e != cudaSuccess) return cuda_fail((c), _e, #call); \
   } while (0)
 
+// A streamed search (velo_search_begin .. velo_search_end) owns the
+// context's buffers while it runs: every other call that stages, launches or
+// reads results waits for velo_search_end.
+bool streaming_refused(velo_ctx* c) {
+  if (!c->streaming) return false;
+  c->err = "a streamed search is in flight: call velo_search_end first";
+  return true;
+}
+
 velo_status ensure(velo_ctx* c, DevBuf& b, size_t bytes, const char* what) {
   if (bytes == 0) bytes = 16;
   if (bytes <= b.cap) return VELO_OK;
@@ -457,6 +466,7 @@ namespace {
 velo_status stage_impl(velo_ctx* c, const uint8_t* buf, const uint64_t* offsets, const uint64_t* sizes,
                        int32_t n, bool direct, bool pageable) {
   if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
+  if (streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   HostTimer timer(&c->stats.host_stage_ms);
   VELO_CUDA(c, cudaSetDevice(c->device));
   c->io_input = nullptr;
@@ -812,6 +822,7 @@ velo_status enqueue_run(velo_ctx* c, const velo_options& o, uint32_t smem) {
 }  // namespace
 
 velo_status velo_run(velo_ctx* c, const velo_options* opts) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
   HostTimer timer(&c->stats.host_launch_ms);
@@ -840,6 +851,7 @@ velo_status velo_synchronize(velo_ctx* c) {
 
 velo_status velo_fetch(velo_ctx* c, velo_track* tracks_out, uint64_t capacity, uint32_t* counts,
                        uint64_t* first, uint32_t* status) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->ran) return VELO_ERR_NOT_STAGED;
   VELO_CUDA(c, cudaSetDevice(c->device));
@@ -1077,6 +1089,7 @@ velo_status velo_search_packed(velo_ctx* c, const uint8_t* buf, const uint64_t* 
                                const uint64_t* sizes, int32_t n, const velo_options* opts,
                                velo_track* tracks_out, uint64_t capacity, uint32_t* counts,
                                uint64_t* first, uint32_t* status) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || n < 0 || (n > 0 && (!buf || !offsets || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
   if (!opts || opts->pipeline_events <= 0) {
     const int32_t part = budget_part(c, sizes, n, opts ? opts->device_budget_mb : 0);
@@ -1283,6 +1296,7 @@ extern "C" {
 velo_status velo_search(velo_ctx* c, const uint8_t* const* events, const uint64_t* sizes, int32_t n,
                         const velo_options* opts, velo_track* tracks_out, uint64_t capacity,
                         uint32_t* counts, uint64_t* first, uint32_t* status) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || n < 0 || (n > 0 && (!events || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
   VELO_CUDA(c, cudaSetDevice(c->device));
   std::vector<uint64_t> offs;
@@ -1309,6 +1323,7 @@ velo_status velo_search(velo_ctx* c, const uint8_t* const* events, const uint64_
 velo_status velo_sort_search(velo_ctx* c, uint8_t* const* events, const uint64_t* sizes, int32_t n,
                              const velo_options* opts, velo_track* tracks_out, uint64_t capacity,
                              uint32_t* counts, uint64_t* first, uint32_t* status) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || n < 0 || (n > 0 && (!events || !sizes))) return VELO_ERR_INVALID_ARGUMENT;
   velo_options o;
   velo_status st = check_options(c, opts, &o);
@@ -1408,6 +1423,7 @@ velo_status velo_search_begin(velo_ctx* c, uint8_t* const* events, const uint64_
 velo_status velo_search_end(velo_ctx* c, uint32_t* counts, uint64_t* first, uint32_t* status) {
   if (!c) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->streaming) return VELO_ERR_NOT_STAGED;
+  c->streaming = false;   // the fetch below is this search's own
   velo_status st = velo_fetch(c, nullptr, 0, counts, first, status);   // waits for the sort and the search
   if (st == VELO_OK)
     for (int32_t e = 0; e < c->n; ++e)
@@ -1421,6 +1437,7 @@ velo_status velo_search_end(velo_ctx* c, uint32_t* counts, uint64_t* first, uint
 
 velo_status velo_time_runs(velo_ctx* c, const velo_options* opts, int32_t warmup, int32_t iters,
                            int32_t flush_l2, float* ms_out) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || iters <= 0 || warmup < 0 || !ms_out) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
   velo_options o;
@@ -1456,6 +1473,7 @@ velo_status velo_time_runs(velo_ctx* c, const velo_options* opts, int32_t warmup
 
 velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, velo_options* best_out,
                           float* best_ms_out) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || !best_out || iters <= 0) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
   velo_options b0;
@@ -1526,6 +1544,7 @@ velo_status velo_autotune(velo_ctx* c, const velo_options* base, int32_t iters, 
 }
 
 velo_status velo_sort_staged(velo_ctx* c) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
   VELO_CUDA(c, cudaSetDevice(c->device));
@@ -1538,6 +1557,7 @@ velo_status velo_sort_staged(velo_ctx* c) {
 }
 
 velo_status velo_fit_tracks(velo_ctx* c, velo_track_fit* fits_out, uint64_t capacity) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || (!fits_out && capacity)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->ran) return VELO_ERR_NOT_STAGED;
   VELO_CUDA(c, cudaSetDevice(c->device));
@@ -1563,6 +1583,7 @@ velo_status velo_fit_tracks(velo_ctx* c, velo_track_fit* fits_out, uint64_t capa
 }
 
 velo_status velo_fetch_staged(velo_ctx* c, uint8_t* buf, uint64_t size) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || (!buf && size)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
   if (size < c->input_bytes) {
@@ -1578,6 +1599,7 @@ velo_status velo_fetch_staged(velo_ctx* c, uint8_t* buf, uint64_t size) {
 
 velo_status velo_set_mlp(velo_ctx* c, const float* weights, float keep_threshold, float window_margin,
                          float min_keep_rate, uint32_t max_event_hits) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || !weights) return VELO_ERR_INVALID_ARGUMENT;
   VELO_CUDA(c, cudaSetDevice(c->device));
   velo_status st = ensure(c, c->d_mlp, sizeof(float) * VELO_MLP_PARAMS, "mlp");
@@ -1597,6 +1619,7 @@ velo_status velo_set_mlp(velo_ctx* c, const float* weights, float keep_threshold
 
 velo_status velo_dump_doublets(velo_ctx* c, const velo_options* opts, uint32_t keep_one_in, float* features_out,
                                uint32_t* ids_out, uint64_t capacity, uint64_t* count_out) {
+  if (c && streaming_refused(c)) return VELO_ERR_INVALID_ARGUMENT;
   if (!c || (capacity && (!features_out || !ids_out))) return VELO_ERR_INVALID_ARGUMENT;
   if (!c->staged) return VELO_ERR_NOT_STAGED;
   velo_options o;

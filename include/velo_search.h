@@ -213,7 +213,8 @@ velo_status velo_sort_search(velo_ctx* ctx, uint8_t* const* events, const uint64
  * read finished events; track_capacity must be at least
  * velo_track_capacity() of the batch.  velo_search_end waits for the
  * search (and the sort's write-back) and returns the per-event outputs and
- * the status of velo_search.
+ * the status of velo_search.  Until then every other call on the context
+ * that stages, launches or fetches returns VELO_ERR_INVALID_ARGUMENT.
  */
 typedef struct velo_event_result {
   uint64_t first;        /* first track of the event in tracks_out */

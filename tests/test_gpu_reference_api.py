@@ -202,6 +202,11 @@ def test_streamed_search_call_order(gpu_ctx, oracle_lib):
     with pytest.raises(native.VeloError) as err:
         gpu_ctx.search_begin(bufs)                          # one streamed search at a time
     assert err.value.status == native.ERR_INVALID_ARGUMENT
+    for call in (lambda: gpu_ctx.search(bufs), lambda: gpu_ctx.run(), lambda: gpu_ctx.fetch_counts(len(bufs)),
+                 lambda: gpu_ctx.sort_search([bytearray(b) for b in bufs])):
+        with pytest.raises(native.VeloError) as err:        # the in-flight search owns the context
+            call()
+        assert err.value.status == native.ERR_INVALID_ARGUMENT
     counts, _, _ = gpu_ctx.search_end(len(bufs))
     assert results["ready"].all() and np.array_equal(counts, results["count"])
     got, _ = gpu_ctx.search(bufs)                            # the context works on
