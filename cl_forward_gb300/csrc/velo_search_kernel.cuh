@@ -34,12 +34,18 @@
 //
 // Per module iteration the CTA meets at two barriers: after forwarding (its
 // used-hit marks feed seeding) and after seeding (its tracklets feed the next
-// forwarding).  Seeding gives each h0 to one warp, whose lanes take the h0's
-// h1 candidates; lane cut-offs come from a ballot and the winner from a warp
-// min-reduction, so seeding itself needs no block barrier.  Each
+// forwarding).  Seeding gives each h0 to a group of G lanes of a warp (G =
+// 8, 16 or 32, the kernel build's seeding width), whose lanes take the h0's
+// h1 candidates; lane cut-offs come from a ballot and the winner from a
+// group min-reduction, so seeding itself needs no block barrier.  Each
 // tracks-to-follow buffer is filled from both ends (forwarding from the
 // front, seeding from the back), which keeps the two counts separate without
 // another barrier.
+//
+// Optional per launch: the x-sort of each event while it is staged, with the
+// sorted hit arrays written back into the input (sort_events), and a
+// per-event record published in host memory when the event is done
+// (results, for a host that consumes events while the search runs).
 #pragma once
 
 #include <cuda_runtime.h>
