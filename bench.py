@@ -857,17 +857,28 @@ def gpu_arm(args, ranks: Ranks):
                         "reference_evals_per_s": (wk["window_evals"] + wk["forward_fits"] + wk["seed_fits"])
                         * value, "counted_by": "oracle restatement on 500 of the events"}
     if ranks.rank == 0 and args.gpus == 1 and not args.no_reference_api:
-        line["e2e_reference_api"] = reference_api_leg(raw, blobs, int(T.sum()), args)
+        line["e2e_reference_api"] = optional_leg(reference_api_leg, raw, blobs, int(T.sum()), args)
     ctx.host_free(hbuf)
     ctx.host_free(h_tracks.view(np.uint8))
     ctx.close()
     if ranks.rank == 0 and args.gpus == 1 and args.config == "scale":
         del raw, blobs
         if not args.no_batched:
-            line["batched"] = batched_leg(args, peak, peak_src)
+            line["batched"] = optional_leg(batched_leg, args, peak, peak_src)
         if not args.no_stress and os.path.exists(LEARNED_WEIGHTS):
-            line["stress"] = stress_leg(args)
+            line["stress"] = optional_leg(stress_leg, args)
     return line if ranks.rank == 0 else None
+
+
+def optional_leg(fn, *a):
+    """A leg beside the headline: its failure is reported in the line
+    (with the error) instead of costing the line itself."""
+    try:
+        return fn(*a)
+    except Exception as exc:   # noqa: BLE001 -- reported, not hidden
+        import traceback
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{type(exc).__name__}: {exc}"[:500]}
 
 
 def main():
