@@ -88,11 +88,23 @@ def gpuPixelSearchByTriplet(input: Sequence, output: List) -> int:
 
 
 def independent_execute(input: Sequence, output: List) -> int:
-    """Standalone entry: x-sort in place, then search (GpuPixelSearchByTriplet.cpp:4-22)."""
+    """Standalone entry: x-sort in place, then search (GpuPixelSearchByTriplet.cpp:4-22).
+
+    As in the library's C++ entry point, the sort runs on the GPU with the
+    reference's permutation (velo_sort_search), in chunks of 16000 events,
+    and leaves the input buffers sorted."""
     global verbosity
     verbosity = 3
-    preorder_by_x(input)
-    return gpuPixelSearchByTripletInvocation(input, output)
+    for ev in input:
+        if isinstance(ev, bytes):
+            raise TypeError("independent_execute sorts in place: pass bytearray or numpy uint8 buffers")
+    output[:] = [b""] * len(input)
+    for i in range(0, len(input), MAX_EVENTS_PER_KERNEL):
+        chunk = list(input[i:i + MAX_EVENTS_PER_KERNEL])
+        tracks, _ = context().sort_search(chunk, native.default_options(host_direct=1))
+        for k, t in enumerate(tracks):
+            output[i + k] = t.tobytes()
+    return 0
 
 
 def independent_post_execute(output: Sequence) -> None:
