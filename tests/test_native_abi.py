@@ -146,3 +146,20 @@ def test_default_options(native_lib):
     assert o.learned == 0 and o.pipeline_events == 0 and o.host_direct == 0 and o.use_graph == 0
     o = native.default_options(y_lanes=2, launch_mode=native.LAUNCH_PER_EVENT)
     assert o.y_lanes == 2 and o.launch_mode == 0
+
+
+def test_python_mirror_refuses_immutable_input():
+    """The reference sorts its input in place: the Python mirror's
+    independent_execute and preorder_by_x refuse `bytes` (immutable) before
+    any device work."""
+    from cl_forward_gb300 import generator, search
+    blob = generator.generate([3])[0][0]
+    with pytest.raises(TypeError):
+        search.independent_execute([blob], [])
+    with pytest.raises(TypeError):
+        search.preorder_by_x([blob])
+    buf = bytearray(blob)
+    search.preorder_by_x([buf])                      # host sort, no GPU needed
+    from oracle import oracle
+    oracle.build()
+    assert bytes(buf) == oracle.sort_by_x(blob)
